@@ -1,0 +1,307 @@
+// C-ABI entry points (include/nsmp.h).  Every function catches host
+// exceptions and returns a status; nothing throws across the boundary.
+#include <cstring>
+#include <new>
+
+#include "ctx.h"
+
+using nsmp::HostLayout;
+
+namespace {
+
+int set_err(nsmp_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+bool valid_field(int f) { return f >= 0 && f < NSMP_NFIELDS; }
+
+}  // namespace
+
+extern "C" {
+
+int nsmp_create(const nsmp_params* prm, const nsmp_mesh* mesh, nsmp_ctx** out) {
+    if (!prm || !mesh || !out || !mesh->No_vp || !mesh->No_cp || !mesh->nbe || !mesh->nbev || !mesh->xv ||
+        !mesh->yv)
+        return NSMP_ERR_ARG;
+    *out = nullptr;
+    nsmp_ctx* c = new (std::nothrow) nsmp_ctx();
+    if (!c) return NSMP_ERR_NOMEM;
+    try {
+        c->prm = *prm;
+        c->device = prm->device;
+        if (prm->precision != NSMP_FP64) {
+            delete c;
+            return NSMP_ERR_UNSUPPORTED;
+        }
+        std::string err;
+        int rc = nsmp::build_layout(*prm, *mesh, c->L, err);
+        if (rc != 0) {
+            delete c;
+            return rc;
+        }
+        rc = nsmp::ctx_init_device(c);
+        if (rc != 0) {
+            nsmp::ctx_free(c);
+            delete c;
+            return rc;
+        }
+    } catch (const std::bad_alloc&) {
+        delete c;
+        return NSMP_ERR_NOMEM;
+    } catch (...) {
+        delete c;
+        return NSMP_ERR_ARG;
+    }
+    *out = c;
+    return NSMP_OK;
+}
+
+int nsmp_destroy(nsmp_ctx* c) {
+    if (!c) return NSMP_ERR_ARG;
+    nsmp::ctx_free(c);
+    delete c;
+    return NSMP_OK;
+}
+
+const char* nsmp_last_error(const nsmp_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int nsmp_ncell(const nsmp_ctx* c, int* n_cell) {
+    if (!c || !n_cell) return NSMP_ERR_ARG;
+    *n_cell = c->L.NC;
+    return NSMP_OK;
+}
+
+void* nsmp_stream(nsmp_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int nsmp_user_initial(nsmp_ctx* c, const double* u, const double* v, const double* w, const double* p) {
+    if (!c || !u || !v || !w || !p) return NSMP_ERR_ARG;
+    const double* in[4] = {u, v, w, p};
+    for (int f = 0; f < 4; ++f) {
+        int rc = nsmp::run_scatter(c, in[f], c->lvl[c->ln][f]);
+        if (rc) return rc;
+    }
+    c->flag_ab = 0;
+    c->lknown = c->ln;
+    return nsmp::run_user_initial(c);
+}
+
+int nsmp_upload_state(nsmp_ctx* c, const double* u, const double* v, const double* w, const double* p,
+                      const double* u1f, const double* u2f, const double* u3f, const double* utf,
+                      const double* ubf, const double* rhsu, const double* rhsv, const double* rhsw, int flag_ab) {
+    if (!c || !u || !v || !w || !p || !u1f || !u2f || !u3f || !utf || !ubf || !rhsu || !rhsv || !rhsw)
+        return NSMP_ERR_ARG;
+    const double* cells[4] = {u, v, w, p};
+    for (int f = 0; f < 4; ++f) {
+        int rc = nsmp::run_scatter(c, cells[f], c->lvl[c->ln][f]);
+        if (rc) return rc;
+    }
+    int rc = nsmp::run_fill_ghosts(c, c->ln);
+    if (rc) return rc;
+    // face fluxes are (N0,NZ): same layout as the interior rows of a cell field
+    const double* faces[5] = {u1f, u2f, u3f, utf, ubf};
+    const int ncell = c->L.NC;
+    for (int f = 0; f < 5; ++f) {
+        // widen (N0,NZ) to (N_CELL,NZ) rows on the host side of the staging copy
+        std::vector<double> tmp((size_t)ncell * c->L.NZ, 0.0);
+        for (int k = 0; k < c->L.NZ; ++k)
+            std::memcpy(&tmp[(size_t)k * ncell], faces[f] + (size_t)k * c->L.N0, sizeof(double) * c->L.N0);
+        rc = nsmp::run_scatter(c, tmp.data(), c->face[f]);
+        if (rc) return rc;
+    }
+    const double* hs[3] = {rhsu, rhsv, rhsw};
+    for (int f = 0; f < 3; ++f) {
+        rc = nsmp::run_scatter(c, hs[f], c->hist[f]);
+        if (rc) return rc;
+    }
+    c->flag_ab = flag_ab;
+    c->lknown = c->ln;
+    return NSMP_OK;
+}
+
+int nsmp_download(nsmp_ctx* c, int field, double* host) {
+    if (!c || !host || !valid_field(field)) return NSMP_ERR_ARG;
+    const int NC = c->L.NC, N0 = c->L.N0;
+    switch (field) {
+        case NSMP_F_U: case NSMP_F_V: case NSMP_F_W: case NSMP_F_P:
+            return nsmp::run_gather(c, c->lvl[c->ln][field - NSMP_F_U], 0, NC, host);
+        case NSMP_F_UNP: case NSMP_F_VNP: case NSMP_F_WNP: case NSMP_F_PNP:
+            return nsmp::run_gather(c, c->lvl[c->lnp][field - NSMP_F_UNP], 0, NC, host);
+        case NSMP_F_U1FACE: case NSMP_F_U2FACE: case NSMP_F_U3FACE: case NSMP_F_UTFACE: case NSMP_F_UBFACE:
+            return nsmp::run_gather(c, c->face[field - NSMP_F_U1FACE], 0, N0, host);
+        case NSMP_F_RHSU: case NSMP_F_RHSV: case NSMP_F_RHSW:
+            return nsmp::run_gather(c, c->hist[field - NSMP_F_RHSU], 1, NC, host);
+        case NSMP_F_EDDY:
+            return nsmp::run_gather(c, c->eddy, 0, NC, host);
+        case NSMP_F_PV:
+            return nsmp::run_download_pv(c, host);
+    }
+    return NSMP_ERR_ARG;
+}
+
+int nsmp_copy_known_from_n(nsmp_ctx* c) {
+    if (!c) return NSMP_ERR_ARG;
+    c->lknown = c->ln;
+    return NSMP_OK;
+}
+
+int nsmp_hydro_stage(nsmp_ctx* c, int* flag_ab, int fin_rk, nsmp_stage_info* info) {
+    if (!c || !flag_ab || fin_rk < 1 || fin_rk > 3) return NSMP_ERR_ARG;
+    c->flag_ab = *flag_ab;
+    int rc;
+    try {
+        rc = nsmp::run_stage(c, fin_rk, info);
+    } catch (...) {
+        return set_err(c, NSMP_ERR_CUDA, "host exception in stage");
+    }
+    *flag_ab = c->flag_ab;
+    return rc;
+}
+
+int nsmp_copy_known_from_np(nsmp_ctx* c) {
+    if (!c) return NSMP_ERR_ARG;
+    c->lknown = c->lnp;
+    return NSMP_OK;
+}
+
+int nsmp_rk2_finalize(nsmp_ctx* c) {
+    if (!c) return NSMP_ERR_ARG;
+    return nsmp::run_combine(c, 0.5, 0.5);
+}
+
+int nsmp_rk_combine(nsmp_ctx* c, double a, double b) {
+    if (!c) return NSMP_ERR_ARG;
+    return nsmp::run_combine(c, a, b);
+}
+
+int nsmp_time_update(nsmp_ctx* c) {
+    if (!c) return NSMP_ERR_ARG;
+    c->ln = c->lnp;
+    c->lknown = c->ln;
+    return NSMP_OK;
+}
+
+// nsmp3D.F90:394-564 for fin_rk 1 and 2; fin_rk 3 is the SSP-RK3
+// composition u1 = S(u^n), u2 = 3/4 u^n + 1/4 S(u1), u^n+1 = 1/3 u^n + 2/3 S(u2)
+// of the same stage (pressure and face fluxes taken from the last stage,
+// as the reference's RK2 does).
+int nsmp_step(nsmp_ctx* c, int fin_rk, int nsteps, nsmp_stage_info* last) {
+    if (!c || fin_rk < 1 || fin_rk > 3 || nsteps < 0) return NSMP_ERR_ARG;
+    int worst = 0;
+    for (int s = 0; s < nsteps; ++s) {
+        nsmp_copy_known_from_n(c);
+        const int nst = fin_rk;
+        nsmp_stage_info inf{};
+        for (int st = 1; st <= nst; ++st) {
+            int fab = c->flag_ab;
+            int rc = nsmp_hydro_stage(c, &fab, fin_rk, &inf);
+            if (rc < 0) return rc;
+            if (rc > worst) worst = rc;
+            if (fin_rk == 3 && st == 2) {
+                rc = nsmp::run_combine(c, 0.75, 0.25);
+                if (rc) return rc;
+            }
+            if (st < nst) nsmp_copy_known_from_np(c);
+        }
+        if (fin_rk == 2) {
+            int rc = nsmp::run_combine(c, 0.5, 0.5);
+            if (rc) return rc;
+        } else if (fin_rk == 3) {
+            int rc = nsmp::run_combine(c, 1.0 / 3.0, 2.0 / 3.0);
+            if (rc) return rc;
+        }
+        nsmp_time_update(c);
+        if (last) *last = inf;
+    }
+    return worst;
+}
+
+int nsmp_mass_diag(nsmp_ctx* c, double out[4]) {
+    if (!c || !out) return NSMP_ERR_ARG;
+    return nsmp::run_mass_diag(c, out);
+}
+
+int nsmp_set_precision(nsmp_ctx* c, int mode) {
+    if (!c) return NSMP_ERR_ARG;
+    if (mode != NSMP_FP64) return set_err(c, NSMP_ERR_UNSUPPORTED, "only NSMP_FP64 is built");
+    c->precision = mode;
+    return NSMP_OK;
+}
+
+int nsmp_prof_enable(nsmp_ctx* c, int on) {
+    if (!c) return NSMP_ERR_ARG;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    nsmp::prof_resolve(c);
+    c->prof_on = on ? 1 : 0;
+    if (on)
+        for (int k = 0; k < NSMP_K_COUNT; ++k) { c->prof_count[k] = 0; c->prof_ms[k] = 0.0; }
+    return NSMP_OK;
+}
+
+int nsmp_prof_read(nsmp_ctx* c, int kid, long long* launches, double* total_ms) {
+    if (!c || kid < 0 || kid >= NSMP_K_COUNT || !launches || !total_ms) return NSMP_ERR_ARG;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    nsmp::prof_resolve(c);
+    *launches = c->prof_count[kid];
+    *total_ms = c->prof_ms[kid];
+    return NSMP_OK;
+}
+
+int nsmp_counters(nsmp_ctx* c, long long* launches, long long* bicg_iters) {
+    if (!c || !launches || !bicg_iters) return NSMP_ERR_ARG;
+    *launches = c->launches;
+    *bicg_iters = c->bicg_iters;
+    return NSMP_OK;
+}
+
+// Host-only diagnostic: geometry exactly as the setup computes it.
+int nsmp_geometry(const nsmp_params* prm, const nsmp_mesh* mesh, int which, double* out, int* count) {
+    if (!prm || !mesh || !out || !count) return NSMP_ERR_ARG;
+    try {
+        HostLayout L;
+        std::string err;
+        int rc = nsmp::build_layout(*prm, *mesh, L, err);
+        if (rc) return rc;
+        const std::vector<double>* src = nullptr;
+        switch (which) {
+            case NSMP_G_XC: src = &L.ref_xc; break;
+            case NSMP_G_YC: src = &L.ref_yc; break;
+            case NSMP_G_AREA: src = &L.ref_area; break;
+            case NSMP_G_DLVV: src = &L.ref_dlVV; break;
+            case NSMP_G_DLCC: src = &L.ref_dlCC; break;
+            case NSMP_G_DLE1: src = &L.ref_dle1; break;
+            case NSMP_G_DLE2: src = &L.ref_dle2; break;
+            case NSMP_G_DOE: src = &L.ref_doe; break;
+            case NSMP_G_XNN: src = &L.ref_xnn; break;
+            case NSMP_G_YNN: src = &L.ref_ynn; break;
+            case NSMP_G_DXCC: src = &L.ref_dxCC; break;
+            case NSMP_G_DYCC: src = &L.ref_dyCC; break;
+            case NSMP_G_SUMXC2: src = &L.ref_sxx; break;
+            case NSMP_G_SUMYC2: src = &L.ref_syy; break;
+            case NSMP_G_SUMXCYC: src = &L.ref_sxy; break;
+            case NSMP_G_SIG: src = &L.sig; break;
+            case NSMP_G_DSIG: src = &L.dsig; break;
+            case NSMP_G_SIGV: src = &L.sigv; break;
+            case NSMP_G_DSIGV: src = &L.dsigv; break;
+            case NSMP_G_DLVSUM: src = &L.ref_dlVsum; break;
+            case NSMP_G_NOCP: {
+                for (size_t q = 0; q < L.ref_No_cp.size(); ++q) out[q] = (double)L.ref_No_cp[q];
+                *count = (int)L.ref_No_cp.size();
+                return NSMP_OK;
+            }
+            case NSMP_G_PERM: {
+                for (size_t q = 0; q < L.perm.size(); ++q) out[q] = (double)L.perm[q];
+                *count = (int)L.perm.size();
+                return NSMP_OK;
+            }
+            default: return NSMP_ERR_ARG;
+        }
+        std::memcpy(out, src->data(), src->size() * sizeof(double));
+        *count = (int)src->size();
+        return NSMP_OK;
+    } catch (...) {
+        return NSMP_ERR_NOMEM;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,78 @@
+// Library context: device-resident state of one solver instance.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "dev.cuh"
+#include "layout.h"
+
+struct nsmp_ctx {
+    nsmp_params prm{};
+    nsmp::HostLayout L;
+    nsmp::Mesh mesh{};
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    int num_sms = 0;
+    std::string err;
+
+    // device tables
+    nsmp::ColPPE* d_ppe = nullptr;
+    nsmp::ColGeo* d_geo = nullptr;
+    int *d_vptr = nullptr, *d_vcell = nullptr;
+    double *d_vcoef = nullptr, *d_lev = nullptr;
+    int *d_gather = nullptr;      // (N_CELL) -> column, for downloads/uploads
+    int *d_vgather = nullptr;     // (N_VERT) -> vertex class
+
+    // state: three buffers per cell field, indexed by time level
+    double* lvl[3][4] = {};       // [buffer][u,v,w,p]
+    int ln = 0, lknown = 0, lnp = 1;
+    double* face[5] = {};         // U1FACE..UBFACE
+    double* hist[3] = {};         // rhsuf, rhsvf, rhswf
+    double* eddy = nullptr;
+    double* ustar[3] = {};
+    double* rhsp = nullptr;
+    double* vtx[4] = {};          // vertex u, v, w, p (tagdir 2, interior layers)
+    // Krylov work vectors
+    double *x = nullptr, *r = nullptr, *r0 = nullptr, *pk = nullptr, *vk = nullptr, *sk = nullptr,
+           *tk = nullptr, *invD = nullptr;
+    double* stage_buf = nullptr;  // (N_CELL,NZ) staging for transfers
+    // reductions and scalars
+    nsmp::RedScratch red{}, red2{};
+    nsmp::Scal* d_scal = nullptr;
+    nsmp::Scal* h_scal = nullptr;  // pinned
+    int flag_ab = 0;
+    int last_iters = 16;
+    int precision = NSMP_FP64;
+    nsmp_stage_info last{};
+    std::vector<void*> allocs;
+    // launch accounting and optional per-kernel event timing
+    long long launches = 0;
+    long long bicg_iters = 0;
+    int prof_on = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<std::pair<int, int>> ev_pending;  // (kernel id, first event index)
+    long long prof_count[NSMP_K_COUNT] = {};
+    double prof_ms[NSMP_K_COUNT] = {};
+};
+
+namespace nsmp {
+
+int ctx_init_device(nsmp_ctx* c);
+void ctx_free(nsmp_ctx* c);
+int run_stage(nsmp_ctx* c, int fin_rk, nsmp_stage_info* info);
+int run_user_initial(nsmp_ctx* c);
+int run_fill_ghosts(nsmp_ctx* c, int buf);
+int run_combine(nsmp_ctx* c, double a, double b);
+int run_gather(nsmp_ctx* c, const double* dfield, int ghost_mode, int rows, double* host);
+int run_scatter(nsmp_ctx* c, const double* host, double* dfield);
+int run_mass_diag(nsmp_ctx* c, double out[4]);
+int run_download_pv(nsmp_ctx* c, double* host);
+int cuda_fail(nsmp_ctx* c, cudaError_t e, const char* where);
+int prof_begin(nsmp_ctx* c, int kid);   // returns event slot or -1
+void prof_end(nsmp_ctx* c, int slot);
+int prof_resolve(nsmp_ctx* c);
+
+}  // namespace nsmp

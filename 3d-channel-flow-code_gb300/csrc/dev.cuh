@@ -1,0 +1,135 @@
+// Device-side data structures and helpers shared by the kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "layout.h"
+
+namespace nsmp {
+
+constexpr int kBlock = 256;   // threads per block of every per-prism kernel
+constexpr int kMaxRed = 4;    // values reduced at once
+
+// Per-layer factor rows of the level table (lev[row*NZ + k0]).
+enum LevRow {
+    LV_DSV = 0, LV_IDSV, LV_IDST, LV_IDSB, LV_IDSBU, LV_WT, LV_WB, LV_GZP, LV_GZM, LV_HMEAN,
+    LV_DD, LV_KD, LV_DAMP, LV_IHZ, LV_COUNT
+};
+
+// Scalars of one stage kept in device memory between kernels.
+struct Scal {
+    double sum_rhs;        // sum of the PPE right-hand side (Glob_Norm, tags = 1)
+    double avec_p;         // volume mean of the solution (Glob_Norm, tags = 0)
+    double max_eddy;
+    double rho, rho_prev, alpha, omega, r0v, ts, tt;
+    double b1, b2, r1, r2, e1, e2;
+    double diag[4];
+    int iter, done, converged, status;
+    int max_iters, pad;
+    double eps;
+};
+
+// Everything a kernel needs to address the mesh; passed by value.
+struct Mesh {
+    int N0, NZ, NZI, nclass;
+    int nprism;            // N0*NZI
+    const ColPPE* ppe;
+    const ColGeo* geo;
+    const int* vptr;
+    const int* vcell;
+    const double* vcoef;
+    const double* lev;     // LV_COUNT x NZ
+    double sgn_bot[3], sgn_top[3];
+    double tv_lsig;        // TotalVolume*(SigFin-SigIni)
+};
+
+// Reduction scratch: per-block partial values and the arrival counter used to
+// elect the last block (which then sums the partials in block order, so the
+// result is deterministic for a fixed grid).
+struct RedScratch {
+    double* partials;      // gridDim.x * kMaxRed
+    unsigned int* counter;
+};
+
+__device__ __forceinline__ double lev(const Mesh& m, int row, int k0) { return __ldg(m.lev + row * m.NZ + k0); }
+
+__device__ __forceinline__ size_t IX(const Mesh& m, int c, int k0) { return (size_t)c * m.NZ + k0; }
+__device__ __forceinline__ size_t IV(const Mesh& m, int v, int k0) { return (size_t)v * m.NZI + (k0 - 1); }
+
+template <int N>
+struct Vec {
+    double v[N];
+};
+
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    return x;
+}
+__device__ __forceinline__ double warp_max(double x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_down_sync(0xffffffffu, x, o));
+    return x;
+}
+
+// Block-wide reduction of N values (sum or max); the result is valid in
+// thread 0.  Fixed tree order: deterministic.
+template <int N, bool MAX>
+__device__ __forceinline__ void block_reduce(double (&x)[N]) {
+    __shared__ double sh[kBlock / 32][N];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < N; ++q) x[q] = MAX ? warp_max(x[q]) : warp_sum(x[q]);
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < N; ++q) sh[wid][q] = x[q];
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int q = 0; q < N; ++q) {
+            double y = (lane < kBlock / 32) ? sh[lane][q] : (MAX ? -INFINITY : 0.0);
+            x[q] = MAX ? warp_max(y) : warp_sum(y);
+        }
+    }
+    __syncthreads();
+}
+
+// Grid reduction: every block contributes x; the last block to arrive gets
+// the totals in `tot` (all its threads) and returns true.  The counter is
+// reset by the last block so the scratch is reusable by the next launch.
+template <int N, bool MAX>
+__device__ bool grid_reduce(double (&x)[N], RedScratch rs, double (&tot)[N]) {
+    __shared__ bool last;
+    block_reduce<N, MAX>(x);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < N; ++q) rs.partials[blockIdx.x * kMaxRed + q] = x[q];
+        __threadfence();
+        unsigned int prev = atomicAdd(rs.counter, 1u);
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double y[N];
+#pragma unroll
+    for (int q = 0; q < N; ++q) y[q] = MAX ? -INFINITY : 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < N; ++q) {
+            double p = __ldcg(rs.partials + b * kMaxRed + q);
+            y[q] = MAX ? fmax(y[q], p) : y[q] + p;
+        }
+    block_reduce<N, MAX>(y);
+    __shared__ double res[N];
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < N; ++q) res[q] = y[q];
+        *rs.counter = 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < N; ++q) tot[q] = res[q];
+    return true;
+}
+
+}  // namespace nsmp

@@ -1,0 +1,920 @@
+// FP64 kernels of one hydro() stage (Main/hydro.F90:197-478) and their
+// orchestration.  Thread mapping of every per-prism kernel: one thread per
+// interior prism (column c, layer k0), layer fastest, so the loads of a warp
+// along a column and along each neighbour column are contiguous.
+//
+// Kernel list of a stage (fused passes, dead reference work dropped):
+//   k_vertex4      cell -> vertex (tagdir 2) of u, v, w and p      BC.F90:202-363
+//   k_stage_rhs    Smagorinsky nu_t + Kim-Choi advection/diffusion
+//                  + Euler/AB2 predictor + wall ghosts of u*       hydro.F90:258-342
+//   k_faces_div    face normal velocities, divergence/dt, PPE
+//                  cross-diffusion RHS, sum for Glob_Norm          source3D.F90:92-127,255-288
+//   k_bicg_init    mean removal, x = pf, r = b - A x, norms        bicgstab.F90:107-451
+//   k_bicg_{p,v,s,t,x}  one BiCGSTAB iteration, dots fused         bicgstab.F90:477-575
+//   k_pmean        volume mean of the solution                     bicgstab.F90:598-666
+//   k_vertex1      cell -> vertex of the corrected pressure        newu3D.F90:119
+//   k_project      LSQ grad p, u = u* - dt grad p, face fluxes      hydro.F90:420-466, newu3D.F90:119-239
+#include <cmath>
+#include <cstdio>
+
+#include "ctx.h"
+
+namespace nsmp {
+namespace {
+
+__device__ __forceinline__ void prism_of(const Mesh& m, int g, int& c, int& k0) {
+    c = g / m.NZI;
+    k0 = 1 + (g - c * m.NZI);
+}
+
+// ---------------------------------------------------------------------------
+// Vertex interpolation: interpolation2D (interpolation2D.F90:120-135) with
+// the periodic averaging of bc_periodic (BC.F90:1243-1300) folded into one
+// stencil per vertex class; tagdir 2 keeps the value at the cell layer.
+// ---------------------------------------------------------------------------
+template <int NF>
+__global__ void __launch_bounds__(kBlock) k_vertex(Mesh m, const double* __restrict__ f0,
+                                                   const double* __restrict__ f1, const double* __restrict__ f2,
+                                                   const double* __restrict__ f3, double* __restrict__ o0,
+                                                   double* __restrict__ o1, double* __restrict__ o2,
+                                                   double* __restrict__ o3, double shift) {
+    const int n = m.nclass * m.NZI;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
+        const int v = g / m.NZI, k0 = 1 + (g - v * m.NZI);
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        const int s1 = __ldg(m.vptr + v + 1);
+        for (int s = __ldg(m.vptr + v); s < s1; ++s) {
+            const double w = __ldg(m.vcoef + s);
+            const size_t q = IX(m, __ldg(m.vcell + s), k0);
+            a0 += w * (f0[q] - shift);
+            if (NF > 1) a1 += w * f1[q];
+            if (NF > 2) a2 += w * f2[q];
+            if (NF > 3) a3 += w * f3[q];
+        }
+        const size_t o = IV(m, v, k0);
+        o0[o] = a0;
+        if (NF > 1) o1[o] = a1;
+        if (NF > 2) o2[o] = a2;
+        if (NF > 3) o3[o] = a3;
+    }
+}
+
+struct StageArgs {
+    const double *u, *v, *w;            // known level (ghost layers valid)
+    const double *uv, *vv, *wv;         // vertex values, tagdir 2
+    const double *f1, *f2, *f3, *fT, *fB; // face fluxes U?FACE
+    double *hu, *hv, *hw;               // AB2 history in/out
+    double *us, *vs, *ws;               // predictor out
+    double* eddy;
+    double c1, c2, dt, inv_re, bdx, bdy, bdz;
+    int les, les_van;
+};
+
+// Kim-Choi face value (interpolationFace.F90:85-111).
+__device__ __forceinline__ double face_val(double phi, double phinb, double kE, double fa, double fb) {
+    return phinb * 0.5 + phi * 0.5 + kE * (fb - fa);
+}
+
+__global__ void __launch_bounds__(kBlock) k_stage_rhs(Mesh m, StageArgs a, RedScratch rs, Scal* sc) {
+    double emax[1] = {0.0};
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const ColGeo& G = m.geo[c];
+        const size_t q = IX(m, c, k0);
+        const double dsv = lev(m, LV_DSV, k0), idsT = lev(m, LV_IDST, k0), idsB = lev(m, LV_IDSB, k0);
+        const double u = a.u[q], v = a.v[q], w = a.w[q];
+        const double uT = a.u[q + 1], vT = a.v[q + 1], wT = a.w[q + 1];
+        const double uB = a.u[q - 1], vB = a.v[q - 1], wB = a.w[q - 1];
+        double unb[3], vnb[3], wnb[3], fu[3], fv[3], fw[3];
+        int nb[3], vx[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            nb[j] = G.nb[j];
+            vx[j] = G.vtx[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const size_t qn = IX(m, nb[j], k0);
+            unb[j] = a.u[qn]; vnb[j] = a.v[qn]; wnb[j] = a.w[qn];
+            const size_t qv = IV(m, vx[j], k0);
+            fu[j] = a.uv[qv]; fv[j] = a.vv[qv]; fw[j] = a.wv[qv];
+        }
+        // face values of the three components (advection and LES gradient)
+        double Uf[3], Vf[3], Wf[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int jj = (j + 1) % 3;
+            Uf[j] = face_val(u, unb[j], G.kE[j], fu[j], fu[jj]);
+            Vf[j] = face_val(v, vnb[j], G.kE[j], fv[j], fv[jj]);
+            Wf[j] = face_val(w, wnb[j], G.kE[j], fw[j], fw[jj]);
+        }
+        const double UT = 0.5 * (u + uT), UB = 0.5 * (u + uB);
+        const double VT = 0.5 * (v + vT), VB = 0.5 * (v + vB);
+        const double WT = 0.5 * (w + wT), WB = 0.5 * (w + wB);
+        // Smagorinsky eddy viscosity (sgm_les.F90:208-250 with fvm_gradient
+        // sgm_les.F90:437-473 and van Driest/Mason damping sgdamp)
+        double gam = a.inv_re, nut = 0.0;
+        if (a.les) {
+            double dudx = 0, dudy = 0, dvdx = 0, dvdy = 0, dwdx = 0, dwdy = 0;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                dudx += Uf[j] * G.lxu[j]; dudy += Uf[j] * G.lyu[j];
+                dvdx += Vf[j] * G.lxv[j]; dvdy += Vf[j] * G.lyv[j];
+                dwdx += Wf[j] * G.lxu[j]; dwdy += Wf[j] * G.lyu[j];
+            }
+            const double ihz = lev(m, LV_IHZ, k0);
+            const double dudz = (UT - UB) * ihz, dvdz = (VT - VB) * ihz, dwdz = (WT - WB) * ihz;
+            const double sxy = 0.5 * (dudy + dvdx), sxz = 0.5 * (dudz + dwdx), syz = 0.5 * (dvdz + dwdy);
+            const double sij = sqrt(2.0 * (dudx * dudx + dvdy * dvdy + dwdz * dwdz) +
+                                    4.0 * (sxy * sxy + sxz * sxz + syz * syz));
+            const double dd = G.cbrt_area * lev(m, LV_DD, k0);
+            double lw = lev(m, LV_KD, k0), l2;
+            if (a.les_van) {
+                if (lw > dd) lw = dd;
+                const double l = lw * lev(m, LV_DAMP, k0);
+                l2 = l * l;
+            } else {
+                l2 = 1.0 / (1.0 / (dd * dd) + 1.0 / (lw * lw));
+            }
+            nut = l2 * sij;
+            gam = nut + a.inv_re;
+            emax[0] = fmax(emax[0], nut);
+        }
+        // diffusion (diffusion3D.F90:110-191; the dle3 term is identically 0)
+        double su = 0.0, sv = 0.0, sw = 0.0;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int jj = (j + 1) % 3;
+            su += (unb[j] - u) * G.kA[j] + (fu[jj] - fu[j]) * G.dle2[j];
+            sv += (vnb[j] - v) * G.kA[j] + (fv[jj] - fv[j]) * G.dle2[j];
+            sw += (wnb[j] - w) * G.kA[j] + (fw[jj] - fw[j]) * G.dle2[j];
+        }
+        const double ar = G.area;
+        su = su * dsv + ((uT - u) * idsT + (uB - u) * idsB) * ar;
+        sv = sv * dsv + ((vT - v) * idsT + (vB - v) * idsB) * ar;
+        sw = sw * dsv + ((wT - w) * idsT + (wB - w) * idsB) * ar;
+        // advection (advection3D.F90:112-284)
+        const double F1 = a.f1[q] * G.L[0] * dsv, F2 = a.f2[q] * G.L[1] * dsv, F3 = a.f3[q] * G.L[2] * dsv;
+        const double FT = a.fT[q] * ar, FB = a.fB[q] * ar;
+        const double au = Uf[0] * F1 + Uf[1] * F2 + Uf[2] * F3 + UT * FT + UB * FB;
+        const double av = Vf[0] * F1 + Vf[1] * F2 + Vf[2] * F3 + VT * FT + VB * FB;
+        const double aw = Wf[0] * F1 + Wf[1] * F2 + Wf[2] * F3 + WT * FT + WB * FB;
+        const double ivol = G.inv_area * lev(m, LV_IDSV, k0);
+        const double ru = a.bdx + gam * su * ivol - au * ivol;
+        const double rv = a.bdy + gam * sv * ivol - av * ivol;
+        const double rw = a.bdz + gam * sw * ivol - aw * ivol;
+        // predictor (hydro.F90:322-333)
+        double pu = a.c1 * ru, pv = a.c1 * rv, pw = a.c1 * rw;
+        if (a.c2 != 0.0) {
+            pu += a.c2 * a.hu[q];
+            pv += a.c2 * a.hv[q];
+            pw += a.c2 * a.hw[q];
+        }
+        const double us = u + a.dt * pu, vs = v + a.dt * pv, ws = w + a.dt * pw;
+        a.us[q] = us; a.vs[q] = vs; a.ws[q] = ws;
+        a.hu[q] = ru; a.hv[q] = rv; a.hw[q] = rw;
+        if (a.les) a.eddy[q] = nut;
+        // wall ghost layers (BCvelcenter3D, BC.F90:459-527; BCpcenter for nu_t)
+        if (k0 == 1) {
+            a.us[q - 1] = m.sgn_bot[0] * us; a.vs[q - 1] = m.sgn_bot[1] * vs; a.ws[q - 1] = m.sgn_bot[2] * ws;
+            if (a.les) a.eddy[q - 1] = nut;
+        }
+        if (k0 == m.NZ - 2) {
+            a.us[q + 1] = m.sgn_top[0] * us; a.vs[q + 1] = m.sgn_top[1] * vs; a.ws[q + 1] = m.sgn_top[2] * ws;
+            if (a.les) a.eddy[q + 1] = nut;
+        }
+    }
+    if (a.les) {
+        double tot[1];
+        if (grid_reduce<1, true>(emax, rs, tot) && threadIdx.x == 0) sc->max_eddy = tot[0];
+    }
+}
+
+struct FaceArgs {
+    const double *us, *vs, *ws;
+    const double* pv;                 // vertex pressure (tagdir 2 of pf)
+    double *f1, *f2, *f3, *fT, *fB;
+    double* rhsp;
+    double inv_dt;
+    int with_div;
+};
+
+// interpolateU (interpolationU.F90:122-160) + source3D divergence
+// (source3D.F90:105-127) + rhsp/dt (hydro.F90:365-373) + update_rhsp
+// (source3D.F90:255-288).
+__global__ void __launch_bounds__(kBlock) k_faces_div(Mesh m, FaceArgs a, RedScratch rs, Scal* sc) {
+    double part[1] = {0.0};
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const ColGeo& G = m.geo[c];
+        const size_t q = IX(m, c, k0);
+        const double u = a.us[q], v = a.vs[q], w = a.ws[q];
+        double U[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const size_t qn = IX(m, G.nb[j], k0);
+            U[j] = (0.5 * (u + a.us[qn])) * G.xn[j] + (0.5 * (v + a.vs[qn])) * G.yn[j];
+        }
+        const double UT = 0.5 * (w + a.ws[q + 1]);
+        const double UB = -1.0 * (0.5 * (w + a.ws[q - 1]));
+        a.f1[q] = U[0]; a.f2[q] = U[1]; a.f3[q] = U[2]; a.fT[q] = UT; a.fB[q] = UB;
+        if (a.with_div) {
+            const double dsv = lev(m, LV_DSV, k0);
+            double div = 0.0;
+            div = div + U[0] * G.L[0] * dsv;
+            div = div + U[1] * G.L[1] * dsv;
+            div = div + U[2] * G.L[2] * dsv;
+            div = div + UT * G.area;
+            div = div + UB * G.area;
+            double r = div * a.inv_dt;
+            double src = 0.0;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const double pa = a.pv[IV(m, G.vtx[j], k0)], pb = a.pv[IV(m, G.vtx[(j + 1) % 3], k0)];
+                src += (pb - pa) * G.dle2[j];
+            }
+            r = r - src * dsv;
+            a.rhsp[q] = r;
+            part[0] += r;
+        }
+    }
+    if (a.with_div) {
+        double tot[1];
+        if (grid_reduce<1, false>(part, rs, tot) && threadIdx.x == 0) sc->sum_rhs = tot[0];
+    }
+}
+
+// PPE row (PDE.F90:69-121) applied to a field: returns sum of the six
+// coefficient products in the reference's order.
+__device__ __forceinline__ double ppe_row(const Mesh& m, const ColPPE& P, int k0, double x0, double x1, double x2,
+                                          double x3, double xT, double xB) {
+    const double dsv = lev(m, LV_DSV, k0);
+    const double AA1 = P.kA[0] * dsv, AA2 = P.kA[1] * dsv, AA3 = P.kA[2] * dsv;
+    const double AAB = P.area * lev(m, LV_IDSB, k0) * lev(m, LV_WB, k0);
+    const double AAT = P.area * lev(m, LV_IDST, k0) * lev(m, LV_WT, k0);
+    const double AA0 = -1.0 * (AAT + AAB + AA1 + AA2 + AA3);
+    return AA0 * x0 + AA1 * x1 + AA2 * x2 + AA3 * x3 + AAT * xT + AAB * xB;
+}
+
+// Jacobi diagonal 1/Am0 (diag_precdt, bicgstab.F90:831-836), once at setup.
+__global__ void k_inv_diag(Mesh m, double* invD) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const ColPPE& P = m.ppe[c];
+        const double dsv = lev(m, LV_DSV, k0);
+        const double AAB = P.area * lev(m, LV_IDSB, k0) * lev(m, LV_WB, k0);
+        const double AAT = P.area * lev(m, LV_IDST, k0) * lev(m, LV_WT, k0);
+        const double AA0 = -1.0 * (AAT + AAB + P.kA[0] * dsv + P.kA[1] * dsv + P.kA[2] * dsv);
+        invD[IX(m, c, k0)] = 1.0 / AA0;
+    }
+}
+
+struct KryArgs {
+    const double* rhsp;
+    const double* pf;
+    double *x, *r, *r0, *p, *v, *s, *t;
+    const double* invD;
+};
+
+// Glob_Norm(rhs, 1) + initial residual and norms (bicgstab.F90:107-109,
+// 403-451).  x = pf is the initial guess (hydro.F90:388-392).
+__global__ void __launch_bounds__(kBlock) k_bicg_init(Mesh m, KryArgs a, RedScratch rs, Scal* sc) {
+    const double avec = sc->sum_rhs / m.tv_lsig;
+    double part[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const ColPPE& P = m.ppe[c];
+        const size_t q = IX(m, c, k0);
+        const double b = a.rhsp[q] - avec * P.area * lev(m, LV_HMEAN, k0);
+        const double x0 = a.pf[q];
+        const double Ax = ppe_row(m, P, k0, x0, a.pf[IX(m, P.nb[0], k0)], a.pf[IX(m, P.nb[1], k0)],
+                                  a.pf[IX(m, P.nb[2], k0)], a.pf[q + 1], a.pf[q - 1]);
+        const double r = b - Ax;
+        a.x[q] = x0;
+        a.r[q] = r;
+        a.r0[q] = r;
+        part[0] += b * b; part[1] += r * r; part[2] += fabs(b); part[3] += fabs(r);
+    }
+    double tot[4];
+    if (grid_reduce<4, false>(part, rs, tot) && threadIdx.x == 0) {
+        double b2 = sqrt(tot[0]), r2 = sqrt(tot[1]), b1 = tot[2], r1 = tot[3];
+        if (b2 == 0.0) b2 = 1.0;
+        if (b1 == 0.0) b1 = 1.0;
+        sc->b1 = b1; sc->b2 = b2; sc->r1 = r1; sc->r2 = r2;
+        sc->e1 = r1 / b1; sc->e2 = r2 / b2;
+        sc->rho = tot[1];
+        sc->rho_prev = 1.0; sc->alpha = 1.0; sc->omega = 1.0;
+        sc->iter = 0;
+        sc->status = 0;
+        sc->converged = 0;
+        sc->done = 0;
+        if (!(r2 == r2)) { sc->status = NSMP_ERR_NAN; sc->done = 1; }
+        else if (sc->e1 < sc->eps || sc->e2 < sc->eps) { sc->converged = 1; sc->done = 1; }
+    }
+}
+
+// update_pk (bicgstab.F90:726-773)
+__global__ void __launch_bounds__(kBlock) k_bicg_p(Mesh m, KryArgs a, const Scal* sc) {
+    if (sc->done) return;
+    const int it = sc->iter;
+    const double beta = (sc->rho / sc->rho_prev) * (sc->alpha / sc->omega), om = sc->omega;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const size_t q = IX(m, c, k0);
+        a.p[q] = (it == 0) ? a.r[q] : a.r[q] + beta * (a.p[q] - om * a.v[q]);
+    }
+}
+
+// y = D^-1 in (diag_precdt), out = A y (get_Apk, bicgstab.F90:976-997) and
+// the fused dot products.  MODE 0: v = A D^-1 p, dot (r0, v);
+// MODE 1: t = A D^-1 s, dots (t, s), (t, t).
+template <int MODE>
+__global__ void __launch_bounds__(kBlock) k_bicg_spmv(Mesh m, KryArgs a, RedScratch rs, Scal* sc) {
+    if (sc->done) return;
+    const double* in = (MODE == 0) ? a.p : a.s;
+    double* out = (MODE == 0) ? a.v : a.t;
+    double part[2] = {0.0, 0.0};
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const ColPPE& P = m.ppe[c];
+        const size_t q = IX(m, c, k0);
+        const size_t q1 = IX(m, P.nb[0], k0), q2 = IX(m, P.nb[1], k0), q3 = IX(m, P.nb[2], k0);
+        const double y0 = in[q] * a.invD[q];
+        const double y1 = in[q1] * a.invD[q1], y2 = in[q2] * a.invD[q2], y3 = in[q3] * a.invD[q3];
+        // wall layers carry zero coefficients (AmB(i,2) = AmT(i,NZ-1) = 0)
+        const double yT = (k0 < m.NZ - 2) ? in[q + 1] * a.invD[q + 1] : 0.0;
+        const double yB = (k0 > 1) ? in[q - 1] * a.invD[q - 1] : 0.0;
+        const double o = ppe_row(m, P, k0, y0, y1, y2, y3, yT, yB);
+        out[q] = o;
+        if (MODE == 0) {
+            part[0] += a.r0[q] * o;
+        } else {
+            const double sv = in[q];
+            part[0] += o * sv;
+            part[1] += o * o;
+        }
+    }
+    double tot[2];
+    if (MODE == 0) {
+        double p1[1] = {part[0]}, t1[1];
+        if (grid_reduce<1, false>(p1, rs, t1) && threadIdx.x == 0) {
+            sc->r0v = t1[0];
+            if (fabs(t1[0]) < 1.0e-30) { sc->done = 1; sc->status = NSMP_WARN_BREAKDOWN; }
+            else sc->alpha = sc->rho / t1[0];
+        }
+    } else {
+        if (grid_reduce<2, false>(part, rs, tot) && threadIdx.x == 0) {
+            sc->ts = tot[0];
+            sc->tt = tot[1];
+            sc->omega = tot[0] / tot[1];
+        }
+    }
+}
+
+// update_sk (bicgstab.F90:1007-1041)
+__global__ void __launch_bounds__(kBlock) k_bicg_s(Mesh m, KryArgs a, const Scal* sc) {
+    if (sc->done) return;
+    const double al = sc->alpha;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const size_t q = IX(m, c, k0);
+        a.s[q] = a.r[q] - al * a.v[q];
+    }
+}
+
+// update_xkrk (bicgstab.F90:1047-1111) + the next rho = (r0, r) and the
+// stopping test of bicgstab.F90:543-566.
+__global__ void __launch_bounds__(kBlock) k_bicg_x(Mesh m, KryArgs a, RedScratch rs, Scal* sc) {
+    if (sc->done) return;
+    const double al = sc->alpha, om = sc->omega;
+    double part[3] = {0.0, 0.0, 0.0};
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const size_t q = IX(m, c, k0);
+        const double id = a.invD[q];
+        const double xn = a.x[q] + al * (a.p[q] * id) + om * (a.s[q] * id);
+        const double res = a.s[q] - om * a.t[q];
+        a.x[q] = xn;
+        a.r[q] = res;
+        part[0] += res * res;
+        part[1] += fabs(res);
+        part[2] += a.r0[q] * res;
+    }
+    double tot[3];
+    if (grid_reduce<3, false>(part, rs, tot) && threadIdx.x == 0) {
+        const double r2 = sqrt(tot[0]), r1 = tot[1];
+        sc->r1 = r1; sc->r2 = r2;
+        sc->e2 = r2 / sc->b2;
+        sc->e1 = r1 / sc->b1;
+        sc->rho_prev = sc->rho;
+        sc->rho = tot[2];
+        sc->iter = sc->iter + 1;
+        double en = 1.0e10;
+        if (en > sc->e1) en = sc->e1;
+        if (en > sc->e2) en = sc->e2;
+        if (!(r2 == r2)) { sc->status = NSMP_ERR_NAN; sc->done = 1; }
+        else if (en < sc->eps) { sc->converged = 1; sc->done = 1; }
+        else if (sc->iter > sc->max_iters) { sc->status = NSMP_WARN_MAXITER; sc->done = 1; }
+        else if (fabs(sc->rho_prev) < 1.0e-30 || fabs(sc->omega) < 1.0e-30) {
+            sc->status = NSMP_WARN_BREAKDOWN; sc->done = 1;
+        }
+    }
+}
+
+// Glob_Norm(phi, 0) sum (bicgstab.F90:617-640)
+__global__ void __launch_bounds__(kBlock) k_pmean(Mesh m, const double* __restrict__ x, RedScratch rs, Scal* sc) {
+    double part[1] = {0.0};
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        part[0] += x[IX(m, c, k0)] * (m.ppe[c].area * lev(m, LV_HMEAN, k0));
+    }
+    double tot[1];
+    if (grid_reduce<1, false>(part, rs, tot) && threadIdx.x == 0) sc->avec_p = tot[0] / m.tv_lsig;
+}
+
+__global__ void k_vertex1(Mesh m, const double* __restrict__ x, const Scal* sc, double* __restrict__ pv) {
+    const double sh = sc->avec_p;
+    const int n = m.nclass * m.NZI;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
+        const int v = g / m.NZI, k0 = 1 + (g - v * m.NZI);
+        double acc = 0.0;
+        const int s1 = __ldg(m.vptr + v + 1);
+        for (int s = __ldg(m.vptr + v); s < s1; ++s) acc += __ldg(m.vcoef + s) * (x[IX(m, __ldg(m.vcell + s), k0)] - sh);
+        pv[IV(m, v, k0)] = acc;
+    }
+}
+
+struct ProjArgs {
+    const double* x;      // BiCGSTAB solution before mean removal
+    const double* pv;     // vertex pressure of the corrected solution
+    const double *us, *vs, *ws;
+    double *f1, *f2, *f3, *fT, *fB;
+    double *un, *vn, *wn, *pn;
+    double dt;
+};
+
+// gradientP(pfnp) (gradientLSM.F90:153-188) + cell correction
+// (hydro.F90:440-448) + newu3D face correction (newu3D.F90:119-239).
+__global__ void __launch_bounds__(kBlock) k_project(Mesh m, ProjArgs a, const Scal* sc) {
+    const double avec = sc->avec_p;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const ColGeo& G = m.geo[c];
+        const size_t q = IX(m, c, k0);
+        const double p = a.x[q] - avec;
+        // wall ghost layers of p are Neumann copies (BCpcenter, BC.F90:869-888)
+        const double pT = (k0 < m.NZ - 2) ? a.x[q + 1] - avec : p;
+        const double pB = (k0 > 1) ? a.x[q - 1] - avec : p;
+        double dpdx = 0.0, dpdy = 0.0, dn[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const double pn = a.x[IX(m, G.nb[j], k0)] - avec;
+            const double d = pn - p;
+            dpdx += G.gx[j] * d;
+            dpdy += G.gy[j] * d;
+            const double va = a.pv[IV(m, G.vtx[j], k0)], vb = a.pv[IV(m, G.vtx[(j + 1) % 3], k0)];
+            dn[j] = d * G.cA[j] + (vb - va) * G.cB[j];
+        }
+        const double dpds = (pT - p) * lev(m, LV_GZP, k0) + (pB - p) * lev(m, LV_GZM, k0);
+        const double un = a.us[q] - a.dt * dpdx, vn = a.vs[q] - a.dt * dpdy, wn = a.ws[q] - a.dt * dpds;
+        a.un[q] = un; a.vn[q] = vn; a.wn[q] = wn; a.pn[q] = p;
+        if (k0 == 1) {
+            a.un[q - 1] = m.sgn_bot[0] * un; a.vn[q - 1] = m.sgn_bot[1] * vn; a.wn[q - 1] = m.sgn_bot[2] * wn;
+            a.pn[q - 1] = p;
+        }
+        if (k0 == m.NZ - 2) {
+            a.un[q + 1] = m.sgn_top[0] * un; a.vn[q + 1] = m.sgn_top[1] * vn; a.wn[q + 1] = m.sgn_top[2] * wn;
+            a.pn[q + 1] = p;
+        }
+        const double dT = (pT - p) * lev(m, LV_IDST, k0);
+        const double dB = (pB - p) * lev(m, LV_IDSBU, k0);
+        a.f1[q] = a.f1[q] - dn[0] * a.dt;
+        a.f2[q] = a.f2[q] - dn[1] * a.dt;
+        a.f3[q] = a.f3[q] - dn[2] * a.dt;
+        a.fT[q] = a.fT[q] - dT * a.dt;
+        a.fB[q] = a.fB[q] - dB * a.dt;
+    }
+}
+
+// Wall ghost layers of a level from its first/last interior layers
+// (BCvelcenter3D/BCpcenter vertical parts).
+__global__ void k_fill_ghosts(Mesh m, double* u, double* v, double* w, double* p) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m.N0; c += gridDim.x * blockDim.x) {
+        const size_t b = (size_t)c * m.NZ, t = b + m.NZ - 1;
+        u[b] = m.sgn_bot[0] * u[b + 1]; v[b] = m.sgn_bot[1] * v[b + 1]; w[b] = m.sgn_bot[2] * w[b + 1];
+        u[t] = m.sgn_top[0] * u[t - 1]; v[t] = m.sgn_top[1] * v[t - 1]; w[t] = m.sgn_top[2] * w[t - 1];
+        p[b] = p[b + 1]; p[t] = p[t - 1];
+    }
+}
+
+__global__ void k_combine(size_t n, double a, double b, const double* __restrict__ un, double* __restrict__ unp) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        unp[i] = a * un[i] + b * unp[i];
+}
+
+// (N_CELL,NZ) Fortran order <-> device columns.  ghost_mode 0: ghost rows
+// copy the periodic image; 1: ghost rows are 0.
+__global__ void k_gather(int ncell, int nz, int layers, int kofs, const int* __restrict__ col,
+                         const double* __restrict__ f, int ghost_mode, int n0, double* __restrict__ out) {
+    const size_t n = (size_t)ncell * layers;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int cell = (int)(i % ncell), k = (int)(i / ncell);
+        double val = f[(size_t)col[cell] * nz + k + kofs];
+        if (ghost_mode == 1 && cell >= n0) val = 0.0;
+        out[i] = val;
+    }
+}
+
+__global__ void k_scatter(int n0, int nz, const int* __restrict__ col, const double* __restrict__ in,
+                          double* __restrict__ f) {
+    const size_t n = (size_t)n0 * nz;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int cell = (int)(i % n0), k = (int)(i / n0);
+        f[(size_t)col[cell] * nz + k] = in[(size_t)cell + (size_t)k * n0];
+    }
+}
+
+// Vertex pressure (N_VERT,NZ-1): layer 1 equals layer 2 because the wall
+// ghost layer of p is a Neumann copy.
+__global__ void k_gather_pv(int nvert, int nzi, const int* __restrict__ vcls, const double* __restrict__ pv,
+                            double* __restrict__ out) {
+    const size_t n = (size_t)nvert * (nzi + 1);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int nv = (int)(i % nvert), k = (int)(i / nvert);  // k = 0..nzi (reference layer k+1)
+        const int kk = (k == 0) ? 0 : k - 1;
+        out[i] = pv[(size_t)vcls[nv] * nzi + kk];
+    }
+}
+
+// glob_cfl mass-flux check (cfl.F90:131-184) with the PPE's cell heights.
+__global__ void __launch_bounds__(kBlock) k_mass_diag(Mesh m, const double* f1, const double* f2, const double* f3,
+                                                      const double* fT, const double* fB, double dt,
+                                                      RedScratch rs, RedScratch rs2, Scal* sc) {
+    double s[2] = {0.0, 0.0}, mx[2] = {0.0, 0.0};
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const ColGeo& G = m.geo[c];
+        const size_t q = IX(m, c, k0);
+        const double dsv = lev(m, LV_DSV, k0);
+        double flux = 0.0;
+        flux = flux + f1[q] * G.L[0] * dsv;
+        flux = flux + f2[q] * G.L[1] * dsv;
+        flux = flux + f3[q] * G.L[2] * dsv;
+        flux = flux + fT[q] * G.area;
+        flux = flux + fB[q] * G.area;
+        double fc = fabs(f1[q] * G.L[0] * dsv) + fabs(f2[q] * G.L[1] * dsv) + fabs(f3[q] * G.L[2] * dsv) +
+                    fabs(fB[q] * G.area) + fabs(fT[q] * G.area);
+        fc = 0.5 * dt * fc * G.inv_area * lev(m, LV_IDSV, k0);
+        s[0] += fabs(flux);
+        s[1] += flux;
+        mx[0] = fmax(mx[0], fabs(flux));
+        mx[1] = fmax(mx[1], fc);
+    }
+    double ts[2], tm[2];
+    if (grid_reduce<2, false>(s, rs, ts) && threadIdx.x == 0) { sc->diag[0] = ts[0]; sc->diag[2] = ts[1]; }
+    // the max reduction uses the second scratch slot: blocks may reach it
+    // while the last block of the sum is still reading its partials
+    if (grid_reduce<2, true>(mx, rs2, tm) && threadIdx.x == 0) { sc->diag[1] = tm[0]; sc->diag[3] = tm[1]; }
+}
+
+int grid_for(const nsmp_ctx* c, long long n) {
+    long long b = (n + kBlock - 1) / kBlock;
+    long long cap = (long long)c->num_sms * 8;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+}  // namespace
+
+int cuda_fail(nsmp_ctx* c, cudaError_t e, const char* where) {
+    c->err = std::string(where) + ": " + cudaGetErrorString(e);
+    return NSMP_ERR_CUDA;
+}
+
+#define CK(call)                                                  \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, #call);    \
+    } while (0)
+#define CKL(where)                                                \
+    do {                                                          \
+        cudaError_t e_ = cudaGetLastError();                      \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, where);    \
+    } while (0)
+
+int prof_begin(nsmp_ctx* c, int kid) {
+    if (!c->prof_on) return -1;
+    if (c->ev_used + 2 > c->ev_pool.size()) {
+        for (int q = 0; q < 256; ++q) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return -1;
+            c->ev_pool.push_back(e);
+        }
+    }
+    const int slot = (int)c->ev_used;
+    c->ev_used += 2;
+    cudaEventRecord(c->ev_pool[slot], c->stream);
+    c->ev_pending.push_back({kid, slot});
+    return slot;
+}
+
+void prof_end(nsmp_ctx* c, int slot) {
+    if (slot < 0) return;
+    cudaEventRecord(c->ev_pool[slot + 1], c->stream);
+}
+
+// Call after the stream has been synchronised.
+int prof_resolve(nsmp_ctx* c) {
+    for (auto& pe : c->ev_pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c->ev_pool[pe.second], c->ev_pool[pe.second + 1]) == cudaSuccess) {
+            c->prof_count[pe.first] += 1;
+            c->prof_ms[pe.first] += ms;
+        }
+    }
+    c->ev_pending.clear();
+    c->ev_used = 0;
+    return 0;
+}
+
+#define LAUNCH(KID, ...)                         \
+    do {                                         \
+        const int slot_ = prof_begin(c, (KID));  \
+        __VA_ARGS__;                             \
+        prof_end(c, slot_);                      \
+        ++c->launches;                           \
+    } while (0)
+
+int run_user_initial(nsmp_ctx* c) {
+    const Mesh& m = c->mesh;
+    double** L = c->lvl[c->ln];
+    const int gb = grid_for(c, m.N0);
+    LAUNCH(NSMP_K_OTHER, k_fill_ghosts<<<gb, kBlock, 0, c->stream>>>(m, L[0], L[1], L[2], L[3]));
+    CKL("k_fill_ghosts");
+    FaceArgs fa{L[0], L[1], L[2], nullptr, c->face[0], c->face[1], c->face[2], c->face[3], c->face[4],
+                nullptr, 0.0, 0};
+    LAUNCH(NSMP_K_OTHER, k_faces_div<<<grid_for(c, m.nprism), kBlock, 0, c->stream>>>(m, fa, c->red, c->d_scal));
+    CKL("k_faces_div(init)");
+    const size_t n = (size_t)m.N0 * m.NZ;
+    for (int q = 0; q < 3; ++q) CK(cudaMemsetAsync(c->hist[q], 0, n * sizeof(double), c->stream));
+    return 0;
+}
+
+int run_fill_ghosts(nsmp_ctx* c, int buf) {
+    double** L = c->lvl[buf];
+    LAUNCH(NSMP_K_OTHER, k_fill_ghosts<<<grid_for(c, c->mesh.N0), kBlock, 0, c->stream>>>(c->mesh, L[0], L[1], L[2], L[3]));
+    CKL("k_fill_ghosts");
+    return 0;
+}
+
+int run_combine(nsmp_ctx* c, double a, double b) {
+    const size_t n = (size_t)c->mesh.N0 * c->mesh.NZ;
+    for (int f = 0; f < 3; ++f) {
+        LAUNCH(NSMP_K_OTHER, k_combine<<<grid_for(c, (long long)n), kBlock, 0, c->stream>>>(n, a, b, c->lvl[c->ln][f], c->lvl[c->lnp][f]));
+        CKL("k_combine");
+    }
+    return 0;
+}
+
+int run_stage(nsmp_ctx* c, int fin_rk, nsmp_stage_info* info) {
+    const Mesh& m = c->mesh;
+    const nsmp_params& P = c->prm;
+    cudaStream_t st = c->stream;
+    // pick the output buffer: neither the known level nor level n
+    int np = 0;
+    while (np == c->lknown || np == c->ln) ++np;
+    c->lnp = np;
+    double** K = c->lvl[c->lknown];
+    double** N = c->lvl[np];
+    const int gp = grid_for(c, m.nprism);
+    const int gv = grid_for(c, (long long)m.nclass * m.NZI);
+    LAUNCH(NSMP_K_VERTEX4, k_vertex<4><<<gv, kBlock, 0, st>>>(m, K[0], K[1], K[2], K[3], c->vtx[0], c->vtx[1], c->vtx[2], c->vtx[3], 0.0));
+    CKL("k_vertex4");
+    StageArgs sa;
+    sa.u = K[0]; sa.v = K[1]; sa.w = K[2];
+    sa.uv = c->vtx[0]; sa.vv = c->vtx[1]; sa.wv = c->vtx[2];
+    sa.f1 = c->face[0]; sa.f2 = c->face[1]; sa.f3 = c->face[2]; sa.fT = c->face[3]; sa.fB = c->face[4];
+    sa.hu = c->hist[0]; sa.hv = c->hist[1]; sa.hw = c->hist[2];
+    sa.us = c->ustar[0]; sa.vs = c->ustar[1]; sa.ws = c->ustar[2];
+    sa.eddy = c->eddy;
+    sa.c1 = (c->flag_ab == 1) ? 1.55 : 1.0;
+    sa.c2 = (c->flag_ab == 1) ? -0.55 : 0.0;
+    sa.dt = P.dt; sa.inv_re = 1.0 / P.re; sa.bdx = P.bdx; sa.bdy = P.bdy; sa.bdz = P.bdz;
+    sa.les = P.les; sa.les_van = P.les_van;
+    LAUNCH(NSMP_K_STAGE_RHS, k_stage_rhs<<<gp, kBlock, 0, st>>>(m, sa, c->red, c->d_scal));
+    CKL("k_stage_rhs");
+    FaceArgs fa{c->ustar[0], c->ustar[1], c->ustar[2], c->vtx[3], c->face[0], c->face[1], c->face[2],
+                c->face[3], c->face[4], c->rhsp, 1.0 / P.dt, 1};
+    LAUNCH(NSMP_K_FACES_DIV, k_faces_div<<<gp, kBlock, 0, st>>>(m, fa, c->red, c->d_scal));
+    CKL("k_faces_div");
+    KryArgs ka{c->rhsp, K[3], c->x, c->r, c->r0, c->pk, c->vk, c->sk, c->tk, c->invD};
+    LAUNCH(NSMP_K_BICG_INIT, k_bicg_init<<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
+    CKL("k_bicg_init");
+    // BiCGSTAB iterations, enqueued in chunks; every kernel returns at once
+    // after the device-side stopping test has fired.
+    int chunk = c->last_iters > 2 ? c->last_iters - 1 : 2;
+    int launched = 0;
+    for (;;) {
+        for (int it = 0; it < chunk; ++it) {
+            LAUNCH(NSMP_K_BICG_P, k_bicg_p<<<gp, kBlock, 0, st>>>(m, ka, c->d_scal));
+            LAUNCH(NSMP_K_BICG_SPMV_V, k_bicg_spmv<0><<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
+            LAUNCH(NSMP_K_BICG_S, k_bicg_s<<<gp, kBlock, 0, st>>>(m, ka, c->d_scal));
+            LAUNCH(NSMP_K_BICG_SPMV_T, k_bicg_spmv<1><<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
+            LAUNCH(NSMP_K_BICG_X, k_bicg_x<<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
+        }
+        CKL("bicgstab iteration");
+        launched += chunk;
+        CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        prof_resolve(c);
+        if (c->h_scal->done) break;
+        if (launched > P.max_iters + 8) {  // cannot happen: the device test stops at MaxIters
+            c->err = "BiCGSTAB did not stop";
+            return NSMP_ERR_CUDA;
+        }
+        chunk = 4;
+    }
+    LAUNCH(NSMP_K_PMEAN, k_pmean<<<gp, kBlock, 0, st>>>(m, c->x, c->red, c->d_scal));
+    CKL("k_pmean");
+    LAUNCH(NSMP_K_VERTEX1, k_vertex1<<<gv, kBlock, 0, st>>>(m, c->x, c->d_scal, c->vtx[3]));
+    CKL("k_vertex1");
+    ProjArgs pa{c->x, c->vtx[3], c->ustar[0], c->ustar[1], c->ustar[2], c->face[0], c->face[1], c->face[2],
+                c->face[3], c->face[4], N[0], N[1], N[2], N[3], P.dt};
+    LAUNCH(NSMP_K_PROJECT, k_project<<<gp, kBlock, 0, st>>>(m, pa, c->d_scal));
+    CKL("k_project");
+    CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    prof_resolve(c);
+    const Scal& s = *c->h_scal;
+    c->last_iters = s.iter > 0 ? s.iter : 1;
+    c->bicg_iters += s.iter;
+    nsmp_stage_info inf{};
+    inf.iters = s.iter;
+    inf.e1norm = s.e1;
+    inf.e2norm = s.e2;
+    inf.converged = s.converged;
+    inf.max_eddy = P.les ? s.max_eddy : 0.0;
+    inf.status = s.status;
+    c->last = inf;
+    if (info) *info = inf;
+    if (fin_rk == 1 && c->flag_ab != 1) c->flag_ab = 1;  // hydro.F90:469-478
+    return s.status;
+}
+
+int run_gather(nsmp_ctx* c, const double* dfield, int ghost_mode, int rows, double* host) {
+    const int ncell = rows;
+    const int layers = c->mesh.NZ;
+    const size_t n = (size_t)ncell * layers;
+    k_gather<<<grid_for(c, (long long)n), kBlock, 0, c->stream>>>(ncell, c->mesh.NZ, layers, 0, c->d_gather,
+                                                                  dfield, ghost_mode, c->L.N0, c->stage_buf);
+    CKL("k_gather");
+    CK(cudaMemcpyAsync(host, c->stage_buf, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int run_download_pv(nsmp_ctx* c, double* host) {
+    const size_t n = (size_t)c->L.NV * (c->mesh.NZI + 1);
+    k_gather_pv<<<grid_for(c, (long long)n), kBlock, 0, c->stream>>>(c->L.NV, c->mesh.NZI, c->d_vgather,
+                                                                     c->vtx[3], c->stage_buf);
+    CKL("k_gather_pv");
+    CK(cudaMemcpyAsync(host, c->stage_buf, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+// host (N_CELL,NZ) interior rows -> device columns
+int run_scatter(nsmp_ctx* c, const double* host, double* dfield) {
+    const int ncell = c->L.NC, n0 = c->L.N0, nz = c->mesh.NZ;
+    // copy the interior rows column by column of the Fortran array
+    for (int k = 0; k < nz; ++k)
+        CK(cudaMemcpyAsync(c->stage_buf + (size_t)k * n0, host + (size_t)k * ncell, n0 * sizeof(double),
+                           cudaMemcpyHostToDevice, c->stream));
+    // stage_buf now holds an (N0,NZ) array; scatter into columns
+    k_scatter<<<grid_for(c, (long long)n0 * nz), kBlock, 0, c->stream>>>(n0, nz, c->d_gather, c->stage_buf, dfield);
+    CKL("k_scatter");
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int run_mass_diag(nsmp_ctx* c, double out[4]) {
+    const Mesh& m = c->mesh;
+    k_mass_diag<<<grid_for(c, m.nprism), kBlock, 0, c->stream>>>(m, c->face[0], c->face[1], c->face[2], c->face[3],
+                                                                c->face[4], c->prm.dt, c->red, c->red2, c->d_scal);
+    CKL("k_mass_diag");
+    CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int q = 0; q < 4; ++q) out[q] = c->h_scal->diag[q];
+    return 0;
+}
+
+int ctx_init_device(nsmp_ctx* c) {
+    CK(cudaSetDevice(c->device));
+    CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    const HostLayout& L = c->L;
+    auto dalloc = [&](void** p, size_t bytes) -> cudaError_t {
+        cudaError_t e = cudaMalloc(p, bytes > 0 ? bytes : 16);
+        if (e == cudaSuccess) c->allocs.push_back(*p);
+        return e;
+    };
+    const size_t ncf = (size_t)L.N0 * L.NZ;
+    const size_t nvf = (size_t)L.nclass * L.NZI;
+    CK(dalloc((void**)&c->d_ppe, sizeof(ColPPE) * L.N0));
+    CK(dalloc((void**)&c->d_geo, sizeof(ColGeo) * L.N0));
+    CK(dalloc((void**)&c->d_vptr, sizeof(int) * L.vptr.size()));
+    CK(dalloc((void**)&c->d_vcell, sizeof(int) * L.vcell.size()));
+    CK(dalloc((void**)&c->d_vcoef, sizeof(double) * L.vcoef.size()));
+    CK(dalloc((void**)&c->d_lev, sizeof(double) * LV_COUNT * L.NZ));
+    CK(dalloc((void**)&c->d_gather, sizeof(int) * L.NC));
+    CK(dalloc((void**)&c->d_vgather, sizeof(int) * L.NV));
+    for (int b = 0; b < 3; ++b)
+        for (int f = 0; f < 4; ++f) CK(dalloc((void**)&c->lvl[b][f], ncf * sizeof(double)));
+    for (auto** p : {&c->face[0], &c->face[1], &c->face[2], &c->face[3], &c->face[4], &c->hist[0], &c->hist[1],
+                     &c->hist[2], &c->eddy, &c->ustar[0], &c->ustar[1], &c->ustar[2], &c->rhsp, &c->x, &c->r,
+                     &c->r0, &c->pk, &c->vk, &c->sk, &c->tk, &c->invD})
+        CK(dalloc((void**)p, ncf * sizeof(double)));
+    for (int f = 0; f < 4; ++f) CK(dalloc((void**)&c->vtx[f], nvf * sizeof(double)));
+    const size_t stage_n = std::max((size_t)L.NC * L.NZ, (size_t)L.NV * L.NZ);
+    CK(dalloc((void**)&c->stage_buf, stage_n * sizeof(double)));
+    const int maxblocks = c->num_sms * 8;
+    CK(dalloc((void**)&c->red.partials, sizeof(double) * kMaxRed * maxblocks));
+    CK(dalloc((void**)&c->red.counter, sizeof(unsigned int)));
+    CK(dalloc((void**)&c->red2.partials, sizeof(double) * kMaxRed * maxblocks));
+    CK(dalloc((void**)&c->red2.counter, sizeof(unsigned int)));
+    CK(dalloc((void**)&c->d_scal, sizeof(Scal)));
+    CK(cudaMallocHost((void**)&c->h_scal, sizeof(Scal)));
+    // zero everything once (face fluxes at the wall layers stay 0, as in the reference)
+    for (int b = 0; b < 3; ++b)
+        for (int f = 0; f < 4; ++f) CK(cudaMemsetAsync(c->lvl[b][f], 0, ncf * sizeof(double), c->stream));
+    for (auto* p : {c->face[0], c->face[1], c->face[2], c->face[3], c->face[4], c->hist[0], c->hist[1], c->hist[2],
+                    c->eddy, c->ustar[0], c->ustar[1], c->ustar[2], c->rhsp, c->x, c->r, c->r0, c->pk, c->vk,
+                    c->sk, c->tk, c->invD})
+        CK(cudaMemsetAsync(p, 0, ncf * sizeof(double), c->stream));
+    CK(cudaMemsetAsync(c->red.counter, 0, sizeof(unsigned int), c->stream));
+    CK(cudaMemsetAsync(c->red2.counter, 0, sizeof(unsigned int), c->stream));
+    CK(cudaMemsetAsync(c->d_scal, 0, sizeof(Scal), c->stream));
+    // tables
+    CK(cudaMemcpyAsync(c->d_ppe, L.ppe.data(), sizeof(ColPPE) * L.N0, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_geo, L.geo.data(), sizeof(ColGeo) * L.N0, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_vptr, L.vptr.data(), sizeof(int) * L.vptr.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_vcell, L.vcell.data(), sizeof(int) * L.vcell.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_vcoef, L.vcoef.data(), sizeof(double) * L.vcoef.size(), cudaMemcpyHostToDevice, c->stream));
+    std::vector<double> lv((size_t)LV_COUNT * L.NZ, 0.0);
+    const Levels& V = L.lev;
+    const std::vector<double>* rows[LV_COUNT] = {&V.dsv, nullptr, &V.idsT, &V.idsB, &V.idsBu, &V.wT, &V.wB,
+                                                 &V.gzp, &V.gzm, &V.hmean, &V.les_dd, &V.les_kd, &V.les_damp, &V.ihz};
+    for (int r = 0; r < LV_COUNT; ++r)
+        for (int k = 0; k < L.NZ; ++k) {
+            if (r == LV_IDSV) lv[(size_t)r * L.NZ + k] = (V.dsv[k] != 0.0) ? 1.0 / V.dsv[k] : 0.0;
+            else lv[(size_t)r * L.NZ + k] = (*rows[r])[k];
+        }
+    CK(cudaMemcpyAsync(c->d_lev, lv.data(), sizeof(double) * lv.size(), cudaMemcpyHostToDevice, c->stream));
+    std::vector<int> gcol(L.NC), vg(L.NV);
+    for (int i = 0; i < L.NC; ++i) gcol[i] = (i < L.N0) ? L.iperm[i] : L.iperm[L.ghost_img[i - L.N0]];
+    for (int v = 0; v < L.NV; ++v) vg[v] = L.vclass[v];
+    CK(cudaMemcpyAsync(c->d_gather, gcol.data(), sizeof(int) * L.NC, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_vgather, vg.data(), sizeof(int) * L.NV, cudaMemcpyHostToDevice, c->stream));
+    // kernel view of the mesh
+    Mesh& m = c->mesh;
+    m.N0 = L.N0; m.NZ = L.NZ; m.NZI = L.NZI; m.nclass = L.nclass;
+    m.nprism = L.N0 * L.NZI;
+    m.ppe = c->d_ppe; m.geo = c->d_geo; m.vptr = c->d_vptr; m.vcell = c->d_vcell; m.vcoef = c->d_vcoef;
+    m.lev = c->d_lev;
+    for (int q = 0; q < 3; ++q) { m.sgn_bot[q] = L.sgn_bot[q]; m.sgn_top[q] = L.sgn_top[q]; }
+    m.tv_lsig = L.total_volume * L.lsig;
+    k_inv_diag<<<grid_for(c, m.nprism), kBlock, 0, c->stream>>>(m, c->invD);
+    CKL("k_inv_diag");
+    Scal s0{};
+    s0.eps = c->prm.eps;
+    s0.max_iters = c->prm.max_iters;
+    CK(cudaMemcpyAsync(c->d_scal, &s0, sizeof(Scal), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+void ctx_free(nsmp_ctx* c) {
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+    c->ev_pool.clear();
+    for (void* p : c->allocs) cudaFree(p);
+    c->allocs.clear();
+    if (c->h_scal) cudaFreeHost(c->h_scal);
+    c->h_scal = nullptr;
+    if (c->stream) cudaStreamDestroy(c->stream);
+    c->stream = nullptr;
+}
+
+}  // namespace nsmp

@@ -1,0 +1,355 @@
+"""Throughput of the nsmp3D hot path on GB300: Mcell-steps/s.
+
+Workload (the 6.3M-prism configuration the headline metric is quoted on):
+periodic channel Lx = 2*pi, Ly = pi, height 2, 256x128 quads split into
+65,536 jittered triangles (mesh seed 0), 96 sigma layers tanh-clustered to
+both walls (beta = 2): 6,291,456 prisms.  Re = 180, dp/dx = -1, Smagorinsky
+Cs = 0.1 with van Driest damping, SSP-RK3 composed of the reference's stage
+operator, dt = 2.5e-4, BiCGSTAB + Jacobi to 1e-10.  Initial state: the
+reference's profile 18 z(2-z) plus uniform noise of half-width 1.8 (seed 1).
+
+One step = one RK3 time step = three hydro() stages, each with its PPE solve.
+All inputs are synthetic (no dataset exists for this path).  Timing: CUDA
+events on the library's stream around K steps after W warm-up steps; the
+working set (~2 GB) is far larger than L2, so no flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(REPO, "3d-channel-flow-code_gb300")
+for _p in (REPO, PKG_DIR):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+WORKLOADS = {
+    # name: (nx, ny, layers, dt)
+    "config0": (32, 16, 32, 1e-3),
+    "config1": (128, 64, 64, 5e-4),
+    "config2": (256, 128, 96, 2.5e-4),
+    "config4": (512, 256, 128, 2.5e-4),
+}
+
+# Algorithmic FP64 words moved per interior prism by each kernel (each named
+# field read or written once; neighbour reads served by cache; geometry
+# amortised per column; vertex fields count N_class/N0 = 0.5 per prism).
+WORDS = {
+    "k_vertex4": 4 + 4 * 0.5, "k_stage_rhs": 3 + 1.5 + 5 + 3 + 3 + 3 + 1, "k_faces_div": 3 + 0.5 + 6,
+    "k_bicg_init": 2 + 3, "k_bicg_p": 4, "k_bicg_spmv_v": 4, "k_bicg_s": 3, "k_bicg_spmv_t": 3,
+    "k_bicg_x": 8, "k_pmean": 1, "k_vertex1": 1 + 0.5, "k_project": 1 + 0.5 + 3 + 5 + 4 + 5,
+}
+# FP64 flops per prism of the solver kernels (multiply, add and FMA counted as
+# 1, 1 and 2 flops; reciprocal of the Jacobi diagonal precomputed).
+FLOPS = {"k_bicg_spmv_v": 33, "k_bicg_spmv_t": 34, "k_bicg_x": 13, "k_bicg_p": 4, "k_bicg_s": 2}
+
+
+def load_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload_desc(name):
+    nx, ny, layers, dt = WORKLOADS[name]
+    return (f"periodic channel 2pi x pi x 2, {nx}x{ny} quads -> {2 * nx * ny} jittered triangles x {layers} "
+            f"tanh(beta=2) layers = {2 * nx * ny * layers} prisms; RK3 dt={dt}; LES van Driest; "
+            f"BiCGSTAB-Jacobi eps=1e-10")
+
+
+def cpu_oracle_sample(name, nthreads, max_seconds=30.0):
+    """Time the CPU oracle on the same workload: the first stage (Euler
+    predictor + full PPE solve) of step 1.  Returns seconds per stage."""
+    import nsmp_gb300 as ng
+    from oracle import oracle_ctypes as oc
+    nx, ny, layers, dt = WORKLOADS[name]
+    mesh = ng.make_mesh(nx, ny)
+    prm = ng.channel_params(nx, ny, layers, dt)
+    okeys = [k for k, _ in oc.OrcParams._fields_ if k != "nthreads"]
+    o = oc.Oracle({k: prm[k] for k in okeys}, mesh, nthreads=nthreads)
+    u, v, w, p = ng.initial_channel(prm, o.ncell, seed=1)
+    o.user_initial(u, v, w, p)
+    t0 = time.perf_counter()
+    _, info = o.step(1)
+    t = time.perf_counter() - t0
+    return t, info
+
+
+def run_reference(args):
+    """CPU arm: the reference's algorithm on the host cores (the oracle port,
+    since no Fortran toolchain exists to build the reference itself)."""
+    world, rank, local, pg = dist_setup()
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    nx, ny, layers, dt = WORKLOADS[args.workload]
+    prisms = 2 * nx * ny * layers
+    for _ in range(args.warmup):
+        cpu_oracle_sample(args.workload, nthreads)
+    times, iters = [], []
+    for _ in range(args.steps):
+        t, info = cpu_oracle_sample(args.workload, nthreads)
+        times.append(t)
+        iters.append(info["iters"])
+    t_stage = float(np.median(times))
+    value = prisms / (3.0 * t_stage) / 1e6
+    line = {
+        "impl": "reference", "metric": "Mcell-steps/s", "value": value, "unit": "Mcell-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 3.0 * t_stage * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_desc(args.workload), "prisms": prisms},
+        "cpu_baseline": {"value": value, "unit": "Mcell-steps/s", "cores": nthreads, "kind": "port",
+                         "sample": "per step: stage 1 of step 1 (predictor + PPE solve to 1e-10, "
+                                   f"{int(np.median(iters))} BiCGSTAB iterations) x3 stages/step"},
+        "e2e": {"value": value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    import nsmp_gb300 as ng
+
+    world, rank, local, pg = dist_setup()
+    torch.cuda.set_device(local)
+    nx, ny, layers, dt = WORKLOADS[args.workload]
+    prisms = 2 * nx * ny * layers
+    mesh = ng.make_mesh(nx, ny)
+    prm = ng.channel_params(nx, ny, layers, dt, device=local)
+    s = ng.Solver(prm, mesh)
+    u0, v0, w0, p0 = ng.initial_channel(prm, s.ncell, seed=1)
+    s.user_initial(u0, v0, w0, p0)
+    stream = torch.cuda.ExternalStream(s.stream)
+    for _ in range(args.warmup):
+        rc, _ = s.step(3, 1)
+        if rc < 0:
+            raise RuntimeError(f"warm-up step failed: {rc}")
+
+    # ---- device-timed region: K steps, inputs resident in HBM -------------
+    s.prof_enable(True)
+    l0, it0 = s.counters()
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    barrier(pg)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    worst = 0
+    for _ in range(args.steps):
+        rc, info = s.step(3, 1)
+        worst = max(worst, rc)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(pg)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    l1, it1 = s.counters()
+    prof = s.prof_read()
+    s.prof_enable(False)
+    ms_max = max_over_ranks(pg, ms)
+    value = world * prisms * args.steps / (ms_max / 1e3) / 1e6
+    iters_per_stage = (it1 - it0) / (3.0 * args.steps)
+
+    # roofline of the dominant kernel (largest share of device time)
+    hbm_peak, peak_kind = load_peaks()
+    dom = max((k for k in prof if k in WORDS), key=lambda k: prof[k][1])
+    n_launch, dom_ms = prof[dom]
+    real_launches = n_launch
+    if dom.startswith("k_bicg_") and dom != "k_bicg_init":
+        real_launches = it1 - it0  # launches after convergence return at once
+    bytes_per_launch = WORDS[dom] * 8.0 * prisms
+    achieved = bytes_per_launch * real_launches / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(REPO, "profiles", "ncu_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            tr = json.load(fh)
+        if dom in tr.get("bytes_per_prism", {}):
+            traffic = tr["bytes_per_prism"][dom] * prisms
+    fl = FLOPS.get(dom)
+    shares = {k: round(v[1] / max(sum(x[1] for x in prof.values()), 1e-12), 4) for k, v in prof.items() if v[0]}
+
+    # ---- end to end through the C-ABI with host buffers -------------------
+    pin = lambda shape: torch.empty(shape[::-1], dtype=torch.float64, pin_memory=True).numpy().T
+    nc, nz = s.ncell, s.nz
+    h_cells = [pin((nc, nz)) for _ in range(4)]
+    h_faces = [pin((prm["n0"], nz)) for _ in range(5)]
+    h_hist = [pin((nc, nz)) for _ in range(3)]
+    for a, f in zip(h_cells, (ng.F_U, ng.F_V, ng.F_W, ng.F_P)):
+        a[...] = s.download(f)
+    for a, f in zip(h_faces, (ng.F_U1FACE, ng.F_U2FACE, ng.F_U3FACE, ng.F_UTFACE, ng.F_UBFACE)):
+        a[...] = s.download(f)
+    for a, f in zip(h_hist, (ng.F_RHSU, ng.F_RHSV, ng.F_RHSW)):
+        a[...] = s.download(f)
+    h_out = [pin((nc, nz)) for _ in range(4)]
+    flag = s.flag_ab
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.upload_state(*h_cells, h_faces, h_hist, flag)
+        s.step(3, 1)
+        for a, f in zip(h_out, (ng.F_U, ng.F_V, ng.F_W, ng.F_P)):
+            a[...] = s.download(f)
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(pg, time.perf_counter() - t0)
+    e2e_value = world * prisms * e2e_steps / t_e2e / 1e6
+    h2d = (4 * nc * nz + 5 * prm["n0"] * nz + 3 * nc * nz) * 8
+    d2h = 4 * nc * nz * 8
+
+    # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        nthreads = os.cpu_count() or 1
+        t_stage, cinfo = cpu_oracle_sample(args.workload, nthreads)
+        cpu = {"value": prisms / (3.0 * t_stage) / 1e6, "unit": "Mcell-steps/s", "cores": nthreads,
+               "kind": "port",
+               "sample": f"stage 1 of step 1 of the same workload ({cinfo['iters']} BiCGSTAB iterations, "
+                         f"{t_stage:.1f} s), scaled x3 stages per step"}
+
+    if rank == 0:
+        line = {
+            "metric": "Mcell-steps/s", "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded mesh and initial state; no dataset exists for this path)",
+            "config": {"workload": workload_desc(args.workload), "prisms": prisms, "precision": "fp64",
+                       "integrator": "SSP-RK3 of the reference stage", "parallelism": "replicas" if world > 1 else "1 GPU",
+                       "l2": "inputs larger than L2 (working set ~2 GB), no flush",
+                       "bicgstab_iters_per_stage": round(iters_per_stage, 1)},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak,
+                         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": bytes_per_launch,
+                         "avg_launch_ms": dom_ms / max(real_launches, 1),
+                         "fp64_tflops": (round(fl * prisms * real_launches / (dom_ms / 1e3) / 1e12, 3)
+                                         if fl and dom_ms > 0 else None)},
+            "kernel_share": shares,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+            "clocks": clk,
+            "gpu_launches": l1 - l0,
+            "status": worst,
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

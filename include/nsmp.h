@@ -1,0 +1,199 @@
+/*
+ * nsmp3D GB300 library -- C-ABI for the per-time-step hot path.
+ *
+ * Drop-in for the Fortran driver of techi28/3D-channel-flow-code: the driver
+ * keeps its setup, I/O and statistics and calls these entry points (through
+ * an ISO_C_BINDING interface block) where it used to call `hydro` and copy
+ * time levels.  Fields stay resident on one GPU between calls.
+ *
+ * Conventions (those of the reference's Fortran arrays):
+ *   - every array argument is a plain host pointer, column-major, with the
+ *     reference's shapes: cell fields (N_CELL,NZ), face fluxes (N0,NZ),
+ *     vertex fields (N_VERT,NZ-1), mesh tables (N0,3);
+ *   - index values inside No_vp/No_cp are 1-based, No_cp = 0 marks a lateral
+ *     boundary edge (data.txt convention, Main/input.F90:150-196);
+ *   - N_CELL = N0 + number of ghost cells (one per lateral boundary edge),
+ *     query it with nsmp_ncell after nsmp_create.
+ * Every entry point returns an int status: 0 ok, > 0 warning (e.g. BiCGSTAB
+ * hit MaxIters), < 0 error.  No host exception crosses the ABI; the text of
+ * the last error is available from nsmp_last_error.  A context is used from
+ * one host thread at a time and owns one CUDA stream.
+ */
+#ifndef NSMP_H
+#define NSMP_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NSMP_OK 0
+#define NSMP_WARN_MAXITER 1      /* BiCGSTAB stopped at MaxIters (bicgstab.F90:562-566) */
+#define NSMP_WARN_BREAKDOWN 2    /* |rho|,|omega| or |r0.v| < 1e-30 (bicgstab.F90:479-517) */
+#define NSMP_ERR_ARG -1          /* bad argument                                        */
+#define NSMP_ERR_MESH -2         /* malformed mesh / periodic pairing failed            */
+#define NSMP_ERR_CUDA -3         /* CUDA runtime error                                  */
+#define NSMP_ERR_NAN -4          /* non-finite residual detected                        */
+#define NSMP_ERR_UNSUPPORTED -5  /* configuration outside the supported key set         */
+#define NSMP_ERR_NOMEM -6        /* device allocation failed                            */
+#define NSMP_ERR_RANGE -7        /* size beyond a documented limit                      */
+
+#define NSMP_FP64 0              /* plain form: FP64 throughout                         */
+#define NSMP_MIXED 1             /* FP32 stencils/Krylov + FP64 iterative refinement    */
+
+/* Runtime parameters: dataParameters.txt (input_parameters.F90:240-442) and
+ * the compile-time constants of common.mpf:59-113 that the path reads. */
+typedef struct nsmp_params {
+    int n0;            /* N_CELL0: interior triangles                          */
+    int nvert;         /* N_VERT                                                */
+    int nz;            /* NZglobal = layers + 2                                 */
+    double xdini, xdfin, ydini, ydfin; /* lateral box (common.mpf:66-69)      */
+    double sigini, sigfin;             /* vertical range (common.mpf:64-65)   */
+    int grid_kind;     /* 0 uniform sigma (calcul_geometry.F90:263-283), 1 tanh */
+    double grid_beta;  /* tanh clustering factor (grid_kind = 1)                */
+    int top_bc;        /* TopBC: 0 no-slip, 1 free-slip                         */
+    int bot_bc;        /* BotBC: 0 no-slip, 1 free-slip                         */
+    double dt, re, bdx, bdy, bdz;
+    double eps;        /* BiCGSTAB tolerance                                    */
+    int max_iters;     /* BiCGSTAB iteration cap                                */
+    int les;           /* 1: Smagorinsky (KeyLES, Iturbu = 1)                   */
+    int les_van;       /* 1: van Driest damping (KeyLESVan), 0: Mason           */
+    int ref_bug_compat;/* 1: reproduce the reference's arithmetic quirks        */
+    int precision;     /* NSMP_FP64 or NSMP_MIXED                               */
+    int device;        /* CUDA device ordinal                                   */
+} nsmp_params;
+
+/* Mesh as read from data.txt (the caller keeps ownership; nothing is
+ * retained after nsmp_create returns). */
+typedef struct nsmp_mesh {
+    const int* No_vp;  /* (N0,3) vertex numbers, counter-clockwise             */
+    const int* No_cp;  /* (N0,3) neighbour across edge j (v_j -> v_j+1), 0 = bd */
+    const int* nbe;    /* (N0) cell tag, != 0 for cells touching the boundary  */
+    const int* nbev;   /* (N_VERT) vertex tag, != 0 on the boundary            */
+    const double* xv;  /* (N_VERT)                                             */
+    const double* yv;  /* (N_VERT)                                             */
+} nsmp_mesh;
+
+typedef struct nsmp_stage_info {
+    int iters;         /* BiCGSTAB iterations                                   */
+    double e1norm;     /* final relative L1 residual                            */
+    double e2norm;     /* final relative L2 residual                            */
+    int converged;     /* 1 if min(e1norm, e2norm) < eps                        */
+    double max_eddy;   /* max nu_t (0 without LES)                              */
+    int status;        /* status of the stage                                   */
+} nsmp_stage_info;
+
+typedef struct nsmp_ctx nsmp_ctx;
+
+/* Field ids for nsmp_download / nsmp_upload_field. */
+enum {
+    NSMP_F_U = 0, NSMP_F_V, NSMP_F_W, NSMP_F_P,        /* level n, (N_CELL,NZ)    */
+    NSMP_F_U1FACE, NSMP_F_U2FACE, NSMP_F_U3FACE,       /* (N0,NZ)                 */
+    NSMP_F_UTFACE, NSMP_F_UBFACE,
+    NSMP_F_RHSU, NSMP_F_RHSV, NSMP_F_RHSW,             /* AB2 history (N_CELL,NZ) */
+    NSMP_F_EDDY,                                       /* nu_t (N_CELL,NZ)        */
+    NSMP_F_UNP, NSMP_F_VNP, NSMP_F_WNP, NSMP_F_PNP,    /* level n+1 (N_CELL,NZ)   */
+    NSMP_F_PV,                                         /* pfv after the stage, (N_VERT,NZ-1) */
+    NSMP_NFIELDS
+};
+
+/* ---- setup: replaces nsmp3D.F90:232-249 device-side ------------------- */
+
+/* Builds the geometry (calcul_geometry, adjust_bc, PDE_center restated),
+ * renumbers columns (reverse Cuthill-McKee) and uploads everything. */
+int nsmp_create(const nsmp_params* prm, const nsmp_mesh* mesh, nsmp_ctx** out);
+int nsmp_destroy(nsmp_ctx* ctx);
+const char* nsmp_last_error(const nsmp_ctx* ctx);
+/* N_CELL = N0 + ghosts, for sizing (N_CELL,NZ) host arrays. */
+int nsmp_ncell(const nsmp_ctx* ctx, int* n_cell);
+
+/* ---- state ------------------------------------------------------------ */
+
+/* user_initial.F90:166-238: level-n cell values in, ghosts filled, face
+ * fluxes from interpolateU, AB2 history zeroed, flag_ab = 0. */
+int nsmp_user_initial(nsmp_ctx* ctx, const double* u, const double* v,
+                      const double* w, const double* p);
+/* Full state upload (restart): cell fields (N_CELL,NZ) at level n, face
+ * fluxes (N0,NZ), AB2 history (N_CELL,NZ). */
+int nsmp_upload_state(nsmp_ctx* ctx, const double* u, const double* v,
+                      const double* w, const double* p, const double* u1f,
+                      const double* u2f, const double* u3f, const double* utf,
+                      const double* ubf, const double* rhsu, const double* rhsv,
+                      const double* rhsw, int flag_ab);
+int nsmp_download(nsmp_ctx* ctx, int field, double* host);
+
+/* ---- time loop: nsmp3D.F90:394-564 ------------------------------------ */
+
+int nsmp_copy_known_from_n(nsmp_ctx* ctx);   /* nsmp3D.F90:419-441 */
+/* One hydro() stage (Main/hydro.F90:8-501).  *flag_ab in/out. */
+int nsmp_hydro_stage(nsmp_ctx* ctx, int* flag_ab, int fin_rk, nsmp_stage_info* info);
+int nsmp_copy_known_from_np(nsmp_ctx* ctx);  /* nsmp3D.F90:480-504 */
+int nsmp_rk2_finalize(nsmp_ctx* ctx);        /* nsmp3D.F90:531-546 */
+/* u,v,w(n+1) = a*u(n) + b*u(n+1) over all cells (SSP-RK3 combinations). */
+int nsmp_rk_combine(nsmp_ctx* ctx, double a, double b);
+int nsmp_time_update(nsmp_ctx* ctx);         /* LoopTimeUpdate.F90:228-250 */
+/* Convenience: nsteps full steps; fin_rk 1 = Euler->AB2, 2 = RK2, 3 = SSP-RK3. */
+int nsmp_step(nsmp_ctx* ctx, int fin_rk, int nsteps, nsmp_stage_info* last);
+
+/* glob_cfl mass-flux reductions (cfl.F90:131-184), FP64 on the device:
+ * out[0] = sum|div|, out[1] = max|div|, out[2] = sum div, out[3] = max CFL. */
+int nsmp_mass_diag(nsmp_ctx* ctx, double out[4]);
+int nsmp_set_precision(nsmp_ctx* ctx, int mode);
+/* Stream used by the context (cudaStream_t as void*). */
+void* nsmp_stream(nsmp_ctx* ctx);
+
+/* ---- instrumentation ---------------------------------------------------- */
+
+/* Kernel ids for nsmp_prof_read. */
+enum {
+    NSMP_K_VERTEX4 = 0, NSMP_K_STAGE_RHS, NSMP_K_FACES_DIV, NSMP_K_BICG_INIT, NSMP_K_BICG_P,
+    NSMP_K_BICG_SPMV_V, NSMP_K_BICG_S, NSMP_K_BICG_SPMV_T, NSMP_K_BICG_X, NSMP_K_PMEAN,
+    NSMP_K_VERTEX1, NSMP_K_PROJECT, NSMP_K_OTHER, NSMP_K_COUNT
+};
+/* on = 1 records a CUDA event pair around every kernel launch on the
+ * context's stream and accumulates per-kernel device time; on = 0 stops.
+ * Enabling also clears the accumulators. */
+int nsmp_prof_enable(nsmp_ctx* ctx, int on);
+int nsmp_prof_read(nsmp_ctx* ctx, int kernel_id, long long* launches, double* total_ms);
+/* Kernels launched and BiCGSTAB iterations executed since creation. */
+int nsmp_counters(nsmp_ctx* ctx, long long* launches, long long* bicg_iters);
+
+/* ---- synthetic inputs (host only, no GPU needed) ------------------------ */
+
+/* Periodic nx x ny quad mesh, each quad split along a seeded diagonal,
+ * interior vertices jittered by +-jitter*spacing.  N0 = 2*nx*ny,
+ * N_VERT = (nx+1)*(ny+1) (boundary vertices duplicated as in the reference). */
+int nsmp_mesh_size(int nx, int ny, int* n0, int* nvert);
+int nsmp_mesh_generate(int nx, int ny, double x0, double x1, double y0,
+                       double y1, double jitter, unsigned long long seed,
+                       int* No_vp, int* No_cp, int* nbe, int* nbev,
+                       double* xv, double* yv);
+/* Seeded channel initial state on the (N_CELL,NZ) grid: u = umax*z*(2-z),
+ * plus uniform noise of half-width amp on u, v, w; p = 0.  The noise of an
+ * interior cell depends only on (seed, original cell number, layer,
+ * component).  Ghost entries are 0 (filled by nsmp_user_initial). */
+int nsmp_initial_channel(const nsmp_params* prm, int n_cell, double umax,
+                         double amp, unsigned long long seed, double* u,
+                         double* v, double* w, double* p);
+/* Sigma grid of the parameters: sig(NZ), dsig(NZ), sigv(NZ-1), dsigv(NZ-1). */
+int nsmp_sigma_grid(const nsmp_params* prm, double* sig, double* dsig,
+                    double* sigv, double* dsigv);
+
+/* Geometry arrays as the setup computes them (calcul_geometry.F90 shapes),
+ * for diagnostics; host only.  `out` must hold 3*N_CELL doubles (N_CELL =
+ * N0 + number of lateral boundary edges); *count receives the length. */
+enum {
+    NSMP_G_XC = 0, NSMP_G_YC, NSMP_G_AREA,                /* (N_CELL)   */
+    NSMP_G_DLVV, NSMP_G_DLCC, NSMP_G_DLE1, NSMP_G_DLE2,   /* (N0,3)     */
+    NSMP_G_DOE, NSMP_G_XNN, NSMP_G_YNN, NSMP_G_DXCC, NSMP_G_DYCC,
+    NSMP_G_SUMXC2, NSMP_G_SUMYC2, NSMP_G_SUMXCYC,         /* (N0)       */
+    NSMP_G_SIG, NSMP_G_DSIG, NSMP_G_SIGV, NSMP_G_DSIGV,   /* sigma grid */
+    NSMP_G_DLVSUM,                                        /* (N_VERT)   */
+    NSMP_G_NOCP,                                          /* (N_CELL,3) */
+    NSMP_G_PERM                                           /* (N0) device column -> cell */
+};
+int nsmp_geometry(const nsmp_params* prm, const nsmp_mesh* mesh, int which,
+                  double* out, int* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1422 @@
+// CPU oracle for the nsmp3D hot path -- TEST INFRASTRUCTURE ONLY.
+//
+// Restates, routine by routine and loop by loop, the serial branches of the
+// Fortran reference (techi28/3D-channel-flow-code) for the shipped key set
+// KeyKimChoi + KeyPPECenter + KeyPPERHS + KeyTESTpBC + KeyTESTChannel, with
+// optional KeyLES/KeyLESVan.  Only tests/, __graft_entry__.smoke() and the CPU
+// baseline leg of bench.py may load it, and only as the checker.
+//
+// Parity with the reference binary is UNPINNED: the reference ships no tests,
+// golden vectors or input decks, and no Fortran toolchain exists here.  Pins
+// available: Functions.F90 analytic fields and the reference's own asserted
+// invariants (see tests/test_oracle.py).
+//
+// Deliberate deviations (all below 1e-15 relative per operation):
+//  * global sums are formed as per-layer partial sums added in layer order
+//    (the reference keeps one running accumulator); this keeps the result
+//    independent of the OpenMP thread count;
+//  * O(N^2) setup searches are restricted to boundary vertices / cells, which
+//    visits the same candidates in the same order and gives identical results.
+//
+// Arrays use Fortran layout through the F2/F1 helpers: A(i,k) with 1-based
+// i, k and the first index fastest, so loops read like the reference's.
+
+#include "nsmp_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+template <class T>
+struct F2 {
+    std::vector<T> d;
+    int n1 = 0, n2 = 0;
+    void init(int a, int b, T v = T()) { n1 = a; n2 = b; d.assign((size_t)a * b, v); }
+    T& operator()(int i, int k) { return d[(size_t)(i - 1) + (size_t)(k - 1) * n1]; }
+    const T& operator()(int i, int k) const { return d[(size_t)(i - 1) + (size_t)(k - 1) * n1]; }
+};
+template <class T>
+struct F1 {
+    std::vector<T> d;
+    void init(int n, T v = T()) { d.assign(n, v); }
+    T& operator()(int i) { return d[(size_t)(i - 1)]; }
+    const T& operator()(int i) const { return d[(size_t)(i - 1)]; }
+};
+typedef F2<double> R2;
+typedef F1<double> R1;
+
+enum { TagBCu = 1, TagBCv = 2, TagBCw = 3, TagBCp = 0 };
+
+}  // namespace
+
+struct orc_ctx {
+    orc_params P;
+    int N0, NV, NZ, NC;  // N_CELL0, N_VERT, NZ, N_CELL (= N_CELLexact)
+    double Lsig;         // SigFin - SigIni
+    // mesh
+    F2<int> No_vp, No_cp;
+    F1<int> nbe, nbev;
+    R1 xv, yv;
+    // geometry (module_geometry.F90)
+    R1 xc, yc, areaCell;
+    R2 dxVV, dyVV, dlVV, xnn, ynn, dxCC, dyCC, dlCC, xe1, ye1, xe2, ye2;
+    R2 dle1, dle2, dle3, xme, yme, xmo, ymo, doe;
+    R1 sum_xc2, sum_yc2, sum_xcyc;
+    R1 sig, dsig, sigv, dsigv;
+    F2<int> surrounding;
+    R2 weight;
+    F1<int> Dimsurrounding, vertex_pair, vertex_edge, TagXC, TagYC, TagXV, TagYV;
+    R1 dlVsum;
+    F1<int> bcuc, bcvc, bcwc, bcpc, bcuv, bcvv, bcwv, bcpv, tagsp;
+    R2 AmC0, AmC1, AmC2, AmC3, AmCT, AmCB;
+    double TotalVolume;
+    int bctop = 1, bcbot = 1;
+    std::vector<int> bnd_cells, bnd_verts, corner_list;
+    // state
+    R2 ufn, vfn, wfn, pfn, uf, vf, wf, pf, ufnp, vfnp, wfnp, pfnp;
+    R2 ufv, vfv, wfv, pfv;
+    R2 U1FACE, U2FACE, U3FACE, UTFACE, UBFACE;
+    R2 rhsuf, rhsvf, rhswf;
+    R2 eddy, walld;
+    int sg_init = 1;
+    int flag_ab = 0;
+    orc_info info{};
+};
+
+namespace {
+
+// Per-layer partial sums added in layer order: deterministic for any
+// thread count.
+template <class F>
+double ksum(int k0, int k1, F f) {
+    std::vector<double> part(k1 - k0 + 1, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int k = k0; k <= k1; ++k) part[k - k0] = f(k);
+    double s = 0.0;
+    for (double x : part) s += x;
+    return s;
+}
+
+// von_Karman = 0.415 is a default-REAL literal assigned to a real*8
+// parameter (module_les.F90:33), so its value is (double)0.415f.
+const double von_Karman = (double)0.415f;
+const double sg_smag_const = 0.1, sg_smag_aplus = 26.0, sg_smag_mason = 2.0,
+             sg_smag_so = 0.0;
+
+// ---------------------------------------------------------------------------
+// Geometry: calcul_geometry.F90 (serial branches), adjust_tagv/adjust_bc
+// (update_bc.F90:4-513) and PDE_center (PDE.F90:69-126).
+// ---------------------------------------------------------------------------
+int build_geometry(orc_ctx& c) {
+    const int N0 = c.N0, NV = c.NV, NZ = c.NZ;
+    const orc_params& P = c.P;
+    // --- sigma grid: calcul_geometry.F90:263-283 ---------------------------
+    c.sigv.init(NZ - 1); c.dsigv.init(NZ - 1); c.sig.init(NZ); c.dsig.init(NZ);
+    if (P.grid_kind == 0) {
+        c.dsigv(1) = (P.sigfin - P.sigini) / (double)(float)(NZ - 2);
+        c.sigv(1) = P.sigini;
+        for (int k = 2; k <= NZ - 2; ++k) {
+            c.dsigv(k) = c.dsigv(1);
+            c.sigv(k) = c.sigv(k - 1) + c.dsigv(k - 1);
+        }
+        c.dsigv(NZ - 1) = c.dsigv(1);
+        c.sigv(NZ - 1) = P.sigfin;
+    } else {
+        // Extension (not in the reference): tanh clustering toward both ends,
+        // z_j = a + (b-a)/2 * (1 - tanh(beta(1-2j/L))/tanh(beta)), j = 0..L.
+        const int L = NZ - 2;
+        const double tb = std::tanh(P.grid_beta);
+        for (int j = 0; j <= L; ++j)
+            c.sigv(j + 1) = P.sigini + 0.5 * (P.sigfin - P.sigini) *
+                                           (1.0 - std::tanh(P.grid_beta * (1.0 - 2.0 * j / L)) / tb);
+        c.sigv(1) = P.sigini;
+        c.sigv(NZ - 1) = P.sigfin;
+        for (int k = 1; k <= NZ - 2; ++k) c.dsigv(k) = c.sigv(k + 1) - c.sigv(k);
+        c.dsigv(NZ - 1) = c.dsigv(NZ - 2);
+    }
+    c.dsig(1) = c.dsigv(1);
+    c.sig(1) = c.sigv(1) - 0.5 * c.dsigv(1);
+    for (int k = 2; k <= NZ - 1; ++k) {
+        c.dsig(k) = 0.5 * (c.dsigv(k) + c.dsigv(k - 1));
+        c.sig(k) = c.sig(k - 1) + c.dsig(k - 1);
+    }
+    c.dsig(NZ) = c.dsigv(NZ - 1);
+    c.sig(NZ) = c.sig(NZ - 1) + c.dsig(NZ - 1);
+
+    // --- per-cell geometry: calcul_geometry.F90:292-367 --------------------
+    // Allocate with the maximal ghost count (one per boundary edge).
+    int nghost_max = 0;
+    for (int i = 1; i <= N0; ++i)
+        for (int j = 1; j <= 3; ++j)
+            if (c.No_cp(i, j) < 1 || c.No_cp(i, j) > N0) ++nghost_max;
+    const int NCmax = N0 + nghost_max;
+    {
+        F2<int> tmp; tmp.init(NCmax, 3, 0);
+        for (int i = 1; i <= N0; ++i)
+            for (int j = 1; j <= 3; ++j) tmp(i, j) = c.No_cp(i, j);
+        c.No_cp = tmp;
+    }
+    c.xc.init(NCmax); c.yc.init(NCmax); c.areaCell.init(NCmax);
+    c.dxVV.init(N0, 3); c.dyVV.init(N0, 3); c.dlVV.init(N0, 3);
+    c.xnn.init(N0, 3); c.ynn.init(N0, 3);
+    double Volsum = 0.0;
+    for (int i = 1; i <= N0; ++i) {
+        int jv1 = c.No_vp(i, 1), jv2 = c.No_vp(i, 2), jv3 = c.No_vp(i, 3);
+        c.xc(i) = (c.xv(jv1) + c.xv(jv2) + c.xv(jv3)) / 3.0;
+        c.yc(i) = (c.yv(jv1) + c.yv(jv2) + c.yv(jv3)) / 3.0;
+        c.areaCell(i) = 0.5 * std::fabs(c.xv(jv1) * (c.yv(jv2) - c.yv(jv3)) +
+                                        c.xv(jv2) * (c.yv(jv3) - c.yv(jv1)) +
+                                        c.xv(jv3) * (c.yv(jv1) - c.yv(jv2)));
+        c.dxVV(i, 1) = c.xv(jv2) - c.xv(jv1);
+        c.dxVV(i, 2) = c.xv(jv3) - c.xv(jv2);
+        c.dxVV(i, 3) = c.xv(jv1) - c.xv(jv3);
+        c.dyVV(i, 1) = c.yv(jv2) - c.yv(jv1);
+        c.dyVV(i, 2) = c.yv(jv3) - c.yv(jv2);
+        c.dyVV(i, 3) = c.yv(jv1) - c.yv(jv3);
+        for (int j = 1; j <= 3; ++j) {
+            c.dlVV(i, j) = std::sqrt(c.dxVV(i, j) * c.dxVV(i, j) + c.dyVV(i, j) * c.dyVV(i, j));
+        }
+        for (int j = 1; j <= 3; ++j) {
+            c.xnn(i, j) = c.dyVV(i, j) / c.dlVV(i, j);
+            c.ynn(i, j) = -c.dxVV(i, j) / c.dlVV(i, j);
+        }
+        Volsum = Volsum + c.areaCell(i);
+    }
+    c.TotalVolume = Volsum;
+
+    // Boundary vertex / cell lists (same ascending order as the full scans).
+    c.bnd_verts.clear(); c.bnd_cells.clear();
+    for (int nv = 1; nv <= NV; ++nv) if (c.nbev(nv) != 0) c.bnd_verts.push_back(nv);
+    for (int i = 1; i <= N0; ++i) if (c.nbe(i) != 0) c.bnd_cells.push_back(i);
+
+    // --- ghost cells with periodic images: calcul_geometry.F90:402-578 -----
+    const double xmin = P.xdini, xmax = P.xdfin, ymin = P.ydini, ymax = P.ydfin;
+    int ii = N0;
+    int vcount = 0;
+    for (int i = 1; i <= N0; ++i) {
+        if (c.nbe(i) > 0) {
+            for (int j = 1; j <= 3; ++j) {
+                int nc = c.No_cp(i, j);
+                if (nc < 1 || nc > N0) {
+                    ii = ii + 1;
+                    c.No_cp(i, j) = ii;
+                    c.No_cp(ii, 1) = i;
+                    c.No_cp(ii, 2) = j;
+                    c.areaCell(ii) = c.areaCell(i);
+                    int jj = j + 1; if (jj > 3) jj -= 3;
+                    int jv1 = c.No_vp(i, j), jv2 = c.No_vp(i, jj);
+                    double xee, yee;
+                    if (std::fabs(c.dyVV(i, j)) < (double)1.0E-7f) {
+                        yee = c.yv(jv2);
+                        xee = c.xc(i);
+                    } else {
+                        double dxody = c.dxVV(i, j) / c.dyVV(i, j);
+                        double dxody2 = dxody * dxody;
+                        yee = (c.yc(i) - (c.xv(jv2) - c.xc(i)) * dxody + c.yv(jv2) * dxody2) / (1.0 + dxody2);
+                        xee = c.xv(jv2) + (yee - c.yv(jv2)) * dxody;
+                    }
+                    c.xc(ii) = 2.0 * xee - c.xc(i);
+                    c.yc(ii) = 2.0 * yee - c.yc(i);
+                    c.No_cp(ii, 3) = -1;
+                    // KeyTESTpBC periodic pairing (XPB = YPB = 1)
+                    double dxl = xmax - xmin, dyl = ymax - ymin;
+                    int jv1p = 0, jv2p = 0, cc = 0;
+                    if (c.xc(ii) > xmax) { dxl = -1.0 * dxl; dyl = 0.; }
+                    else if (c.xc(ii) < xmin) { dxl = dxl; dyl = 0.; }
+                    if (c.yc(ii) > ymax) { dxl = 0.; dyl = -1.0 * dyl; }
+                    else if (c.yc(ii) < ymin) { dxl = 0.; dyl = dyl; }
+                    if (dxl * dyl > (double)1.0E-7f) {
+                        vcount = vcount + 1;
+                    } else {
+                        int ncount = 0;
+                        double xe1 = c.xv(jv1) + dxl, ye1 = c.yv(jv1) + dyl;
+                        for (int nv : c.bnd_verts)
+                            if (std::fabs(xe1 - c.xv(nv)) < (double)1.0E-7f &&
+                                std::fabs(ye1 - c.yv(nv)) < (double)1.0E-7f) { jv1p = nv; ++ncount; }
+                        if (ncount != 1) return -11;  // 'ERROR!VERTEX PAIR FOR JV1'
+                        ncount = 0;
+                        double xe2 = c.xv(jv2) + dxl, ye2 = c.yv(jv2) + dyl;
+                        for (int nv : c.bnd_verts)
+                            if (std::fabs(xe2 - c.xv(nv)) < (double)1.0E-7f &&
+                                std::fabs(ye2 - c.yv(nv)) < (double)1.0E-7f) { jv2p = nv; ++ncount; }
+                        if (ncount != 1) return -12;  // 'ERROR!VERTEX PAIR FOR JV2'
+                        ncount = 0;
+                        for (int i0 : c.bnd_cells) {
+                            long jv10 = c.No_vp(i0, 1), jv20 = c.No_vp(i0, 2), jv30 = c.No_vp(i0, 3);
+                            long pp = (long)jv1p * jv2p;
+                            if (jv10 * jv20 == pp) {
+                                if (jv10 == jv1p) { cc = (int)jv30; c.No_cp(ii, 3) = i0; ++ncount; }
+                                else if (jv10 == jv2p) { cc = (int)jv30; c.No_cp(ii, 3) = i0; ++ncount; }
+                            }
+                            if (jv30 * jv20 == pp) {
+                                if (jv30 == jv1p) { cc = (int)jv10; c.No_cp(ii, 3) = i0; ++ncount; }
+                                else if (jv30 == jv2p) { cc = (int)jv10; c.No_cp(ii, 3) = i0; ++ncount; }
+                            }
+                            if (jv10 * jv30 == pp) {
+                                if (jv10 == jv1p) { cc = (int)jv20; c.No_cp(ii, 3) = i0; ++ncount; }
+                                else if (jv10 == jv2p) { cc = (int)jv20; c.No_cp(ii, 3) = i0; ++ncount; }
+                            }
+                        }
+                        if (ncount != 1) return -13;  // 'ERROR FIND PERIDOIC CELL'
+                        double xq = c.xv(cc) - dxl, yq = c.yv(cc) - dyl;
+                        c.xc(ii) = (c.xv(jv1) + c.xv(jv2) + xq) / 3.0;
+                        c.yc(ii) = (c.yv(jv1) + c.yv(jv2) + yq) / 3.0;
+                    }
+                }
+            }
+        }
+    }
+    if (vcount != 0) return -14;  // only fully periodic lateral boundaries supported
+    c.NC = ii;
+    const int NC = c.NC;
+
+    // --- TagXC/TagYC: calcul_geometry.F90:853-887 ---------------------------
+    c.TagXC.init(NC, 0); c.TagYC.init(NC, 0);
+    for (int i = 1; i <= NC; ++i) {
+        int ncount = 0;
+        if (c.xc(i) < P.xdini) { c.TagXC(i) = 1; ++ncount; }
+        if (c.xc(i) > P.xdfin) { c.TagXC(i) = 2; ++ncount; }
+        if (c.yc(i) < P.ydini) { c.TagYC(i) = 1; ++ncount; }
+        if (c.yc(i) > P.ydfin) { c.TagYC(i) = 2; ++ncount; }
+        if (ncount > 1) return -15;  // 'ERROR IN TAGXC,TAGYC'
+    }
+    // --- TagXV/TagYV: calcul_geometry.F90:893-917 ---------------------------
+    c.TagXV.init(NV, 0); c.TagYV.init(NV, 0);
+    for (int nv = 1; nv <= NV; ++nv) {
+        if (c.nbev(nv) != 0) {
+            double xee = c.xv(nv), yee = c.yv(nv);
+            if (std::fabs(xee - P.xdini) < 1.0e-7) c.TagXV(nv) = 1;
+            if (std::fabs(xee - P.xdfin) < 1.0e-7) c.TagXV(nv) = 2;
+            if (std::fabs(yee - P.ydini) < 1.0e-7) c.TagYV(nv) = 1;
+            if (std::fabs(yee - P.ydfin) < 1.0e-7) c.TagYV(nv) = 2;
+        }
+    }
+    // --- vertex_pair / vertex_edge: calcul_geometry.F90:920-1040 ------------
+    c.vertex_pair.init(NV, -1); c.vertex_edge.init(NV, -1);
+    for (int nv = 1; nv <= NV; ++nv) {
+        double xee = c.xv(nv), yee = c.yv(nv);
+        int ncount;
+        if (c.TagXV(nv) * c.TagYV(nv) > 0) ncount = 2;
+        else if (c.TagXV(nv) > 0) ncount = 1;
+        else if (c.TagYV(nv) > 0) ncount = 1;
+        else ncount = 0;
+        if (ncount == 1) {
+            int vc = 0;
+            for (int i : c.bnd_verts) {
+                // YPB = 1
+                if (std::fabs(xee - c.xv(i)) < 1.0e-7 &&
+                    std::fabs(yee - c.yv(i)) > (P.ydfin - P.ydini - 1.0e-7)) { ++vc; c.vertex_pair(nv) = i; }
+                // XPB = 1
+                if (std::fabs(yee - c.yv(i)) < 1.0e-7 &&
+                    std::fabs(xee - c.xv(i)) > (P.xdfin - P.xdini - 1.0e-7)) { ++vc; c.vertex_pair(nv) = i; }
+            }
+            if (vc == 0) c.vertex_pair(nv) = -1;
+            else if (vc != 1) return -16;  // 'ERROR! MISSING PERIODIC NB'
+        }
+        if (ncount == 2) c.vertex_edge(nv) = 1;  // XPB*YPB = 1
+    }
+    // --- vertex stencil: calcul_geometry.F90:1055-1076 ----------------------
+    // Same order as the reference's scan (cells ascending, then j).
+    {
+        std::vector<int> cnt(NV + 1, 0);
+        for (int i = 1; i <= N0; ++i)
+            for (int j = 1; j <= 3; ++j) cnt[c.No_vp(i, j)]++;
+        int maxs = 0;
+        for (int nv = 1; nv <= NV; ++nv) maxs = std::max(maxs, cnt[nv]);
+        c.surrounding.init(NV, std::max(maxs, 1), 0);
+        c.weight.init(NV, std::max(maxs, 1), 0.0);
+        c.Dimsurrounding.init(NV, 0);
+        c.dlVsum.init(NV, 0.0);
+        for (int i = 1; i <= N0; ++i)
+            for (int j = 1; j <= 3; ++j) {
+                int nv = c.No_vp(i, j);
+                int j0 = ++c.Dimsurrounding(nv);
+                c.surrounding(nv, j0) = i;
+                double dxCV = c.xc(i) - c.xv(nv), dyCV = c.yc(i) - c.yv(nv);
+                c.weight(nv, j0) = 1.0 / std::sqrt(dxCV * dxCV + dyCV * dyCV);
+                c.dlVsum(nv) = c.dlVsum(nv) + c.weight(nv, j0);
+            }
+    }
+    // --- edge points: calcul_geometry.F90:1343-1387 (EdgePointOption = 1) ---
+    c.xme.init(N0, 3); c.yme.init(N0, 3); c.xmo.init(N0, 3); c.ymo.init(N0, 3); c.doe.init(N0, 3);
+    for (int i = 1; i <= N0; ++i)
+        for (int j = 1; j <= 3; ++j) {
+            int jj = j + 1; if (jj > 3) jj -= 3;
+            int jv1 = c.No_vp(i, j), jv2 = c.No_vp(i, jj);
+            c.xme(i, j) = 0.5 * (c.xv(jv2) + c.xv(jv1));
+            c.yme(i, j) = 0.5 * (c.yv(jv2) + c.yv(jv1));
+            int jc = c.No_cp(i, j);
+            double xm1 = c.xc(i), xm2 = c.xc(jc), xm3 = c.xv(jv1), xm4 = c.xv(jv2);
+            double ym1 = c.yc(i), ym2 = c.yc(jc), ym3 = c.yv(jv1), ym4 = c.yv(jv2);
+            c.xmo(i, j) = ((xm1 * ym2 - ym1 * xm2) * (xm3 - xm4) - (xm1 - xm2) * (xm3 * ym4 - ym3 * xm4)) /
+                          ((xm1 - xm2) * (ym3 - ym4) - (ym1 - ym2) * (xm3 - xm4));
+            c.ymo(i, j) = ((xm1 * ym2 - ym1 * xm2) * (ym3 - ym4) - (ym1 - ym2) * (xm3 * ym4 - ym3 * xm4)) /
+                          ((xm1 - xm2) * (ym3 - ym4) - (ym1 - ym2) * (xm3 - xm4));
+            xm1 = c.xme(i, j) - c.xmo(i, j);
+            ym1 = c.yme(i, j) - c.ymo(i, j);
+            c.doe(i, j) = std::sqrt(xm1 * xm1 + ym1 * ym1);
+            xm2 = xm1 * c.dxVV(i, j) + ym1 * c.dyVV(i, j);
+            if (xm2 < 0.0) c.doe(i, j) = -c.doe(i, j);
+        }
+    // --- LSQ sums and Kim-Choi coefficients: calcul_geometry.F90:1460-1517 --
+    c.dxCC.init(N0, 3); c.dyCC.init(N0, 3); c.dlCC.init(N0, 3);
+    c.xe1.init(N0, 3); c.ye1.init(N0, 3); c.xe2.init(N0, 3); c.ye2.init(N0, 3);
+    c.dle1.init(N0, 3); c.dle2.init(N0, 3); c.dle3.init(N0, 3);
+    c.sum_xc2.init(N0); c.sum_yc2.init(N0); c.sum_xcyc.init(N0);
+    for (int i = 1; i <= N0; ++i) {
+        double sumX = 0.0, sumY = 0.0, sumXY = 0.0;
+        for (int j = 1; j <= 3; ++j) {
+            int jc = c.No_cp(i, j);
+            c.dxCC(i, j) = c.xc(jc) - c.xc(i);
+            c.dyCC(i, j) = c.yc(jc) - c.yc(i);
+            c.dlCC(i, j) = std::sqrt(c.dxCC(i, j) * c.dxCC(i, j) + c.dyCC(i, j) * c.dyCC(i, j));
+            sumX = sumX + c.dxCC(i, j) * c.dxCC(i, j);
+            sumY = sumY + c.dyCC(i, j) * c.dyCC(i, j);
+            sumXY = sumXY + c.dxCC(i, j) * c.dyCC(i, j);
+            double nfn1 = c.dxCC(i, j) * c.xnn(i, j) + c.dyCC(i, j) * c.ynn(i, j);
+            c.xe1(i, j) = c.dxCC(i, j) / nfn1;
+            c.ye1(i, j) = c.dyCC(i, j) / nfn1;
+            c.xe2(i, j) = c.xnn(i, j) - c.xe1(i, j);
+            c.ye2(i, j) = c.ynn(i, j) - c.ye1(i, j);
+            // KeyKimChoi
+            double xee = c.dxCC(i, j) / c.dlCC(i, j);
+            double yee = c.dyCC(i, j) / c.dlCC(i, j);
+            nfn1 = xee * c.xnn(i, j) + yee * c.ynn(i, j);
+            xee = xee / nfn1;
+            yee = yee / nfn1;
+            c.dle1(i, j) = 1.0 / nfn1;
+            c.dle3(i, j) = 0.;
+            xee = c.xnn(i, j) - xee;
+            yee = c.ynn(i, j) - yee;
+            nfn1 = xee * c.dxVV(i, j) + yee * c.dyVV(i, j);
+            if (nfn1 < 0.) c.dle2(i, j) = -1.0 * std::sqrt(xee * xee + yee * yee);
+            else c.dle2(i, j) = std::sqrt(xee * xee + yee * yee);
+        }
+        c.sum_xc2(i) = sumX;
+        c.sum_yc2(i) = sumY;
+        c.sum_xcyc(i) = sumXY;
+    }
+    // --- adjust_tagv: update_bc.F90:4-82 (corner priority to y) ------------
+    for (int nv = 1; nv <= NV; ++nv)
+        if (c.nbev(nv) != 0 && c.TagXV(nv) * c.TagYV(nv) != 0) c.TagXV(nv) = 0;
+    // --- adjust_bc: update_bc.F90:86-513 (fully periodic lateral BCs) ------
+    c.tagsp.init(NC, 0);
+    c.bcuc.init(NC, -1); c.bcvc.init(NC, -1); c.bcwc.init(NC, -1); c.bcpc.init(NC, -1);
+    for (int i = 1; i <= N0; ++i)
+        if (c.nbe(i) != 0)
+            for (int j = 1; j <= 3; ++j) {
+                int nc = c.No_cp(i, j);
+                if (nc < 1 || nc > N0) {
+                    int img = c.No_cp(nc, 3);
+                    if (img <= 0) return -17;  // non-periodic ghost: unsupported
+                    c.bcuc(nc) = 3; c.bcvc(nc) = 3; c.bcwc(nc) = 3; c.bcpc(nc) = 3;
+                }
+            }
+    c.bcuv.init(NV, -1); c.bcvv.init(NV, -1); c.bcwv.init(NV, -1); c.bcpv.init(NV, -1);
+    for (int nv = 1; nv <= NV; ++nv)
+        if (c.nbev(nv) != 0) {
+            int flag = 0;
+            if (c.TagXV(nv) > 0) ++flag;  // XPB = 1 -> fB = 3
+            if (c.TagYV(nv) > 0) ++flag;  // YPB = 1 -> fB = 3
+            if (flag != 1) return -18;    // 'FATAL ERROR FOR BC VERTEX'
+            c.bcuv(nv) = 3; c.bcvv(nv) = 3; c.bcwv(nv) = 3; c.bcpv(nv) = 3;
+        }
+    c.corner_list.clear();
+    for (int nv = 1; nv <= NV; ++nv) if (c.vertex_edge(nv) == 1) c.corner_list.push_back(nv);
+    if (c.corner_list.size() != 4) return -19;  // 'ERROR! EDGE POINT MISSING'
+    // --- PDE_center: PDE.F90:69-121 -----------------------------------------
+    c.AmC0.init(N0, NZ); c.AmC1.init(N0, NZ); c.AmC2.init(N0, NZ);
+    c.AmC3.init(N0, NZ); c.AmCT.init(N0, NZ); c.AmCB.init(N0, NZ);
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            double AA[4];
+            for (int j = 1; j <= 3; ++j) {
+                int jc = c.No_cp(i, j);
+                double co1 = c.dle1(i, j) / c.dlCC(i, j);
+                if (c.bcpc(jc) == 1) { AA[j] = 0.0; continue; }
+                AA[j] = co1 * c.dlVV(i, j) * c.dsigv(k - 1);
+            }
+            double AAB = c.areaCell(i) / c.dsig(k - 1);
+            double AAT = c.areaCell(i) / c.dsig(k);
+            if (k == 2 && c.bcbot == 1) AAB = 0.0;
+            if (k == NZ - 1 && c.bctop == 1) AAT = 0.0;
+            double AA0 = -1.0 * (AAT + AAB + AA[1] + AA[2] + AA[3]);
+            c.AmC0(i, k) = AA0; c.AmC1(i, k) = AA[1]; c.AmC2(i, k) = AA[2];
+            c.AmC3(i, k) = AA[3]; c.AmCT(i, k) = AAT; c.AmCB(i, k) = AAB;
+        }
+    // get_matrix_coef (bicgstab.F90:239-288): wall coefficients must vanish.
+    for (int i = 1; i <= N0; ++i) {
+        if (std::fabs(c.AmCT(i, NZ - 1)) > 1.0e-7) return -20;
+        if (std::fabs(c.AmCB(i, 2)) > 1.0e-7) return -21;
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Runtime boundary conditions: BC.F90 serial branches.
+// ---------------------------------------------------------------------------
+
+// BCvelcenter3D: BC.F90:367-594
+void BCvelcenter3D(orc_ctx& c, R2& phi, int tagBC) {
+    const int N0 = c.N0, NZ = c.NZ;
+    if (c.bcbot == 1) {
+        bool neg = (c.P.bot_bc == 0) || (tagBC == 3);
+        for (int i = 1; i <= N0; ++i) phi(i, 1) = neg ? -phi(i, 2) : phi(i, 2);
+    }
+    if (c.bctop == 1) {
+        bool neg = (c.P.top_bc == 0) || (tagBC == 3);
+        for (int i = 1; i <= N0; ++i) phi(i, NZ) = neg ? -phi(i, NZ - 1) : phi(i, NZ - 1);
+    }
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= NZ; ++k)
+        for (int i : c.bnd_cells)
+            for (int j = 1; j <= 3; ++j) {
+                int nc = c.No_cp(i, j);
+                int flag = (tagBC == 1) ? c.bcuc(nc) : (tagBC == 2) ? c.bcvc(nc) : c.bcwc(nc);
+                double fB = 0.0;
+                if (flag == 0) fB = 0. - phi(i, k);
+                if (flag == 1) fB = phi(i, k);
+                if (flag == 3) fB = phi(c.No_cp(nc, 3), k);
+                if (flag != -1) phi(nc, k) = fB;
+            }
+}
+
+// BCpcenter: BC.F90:812-977
+void BCpcenter(orc_ctx& c, R2& phi) {
+    const int N0 = c.N0, NZ = c.NZ;
+    if (c.bctop == 1)
+        for (int i = 1; i <= N0; ++i) phi(i, NZ) = phi(i, NZ - 1);
+    if (c.bcbot == 1)
+        for (int i = 1; i <= N0; ++i) phi(i, 1) = phi(i, 2);
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= NZ; ++k)
+        for (int i : c.bnd_cells)
+            for (int j = 1; j <= 3; ++j) {
+                int nc = c.No_cp(i, j);
+                int flag = c.bcpc(nc);
+                double fB = 0.0;
+                if (flag == 0) fB = -phi(i, k);
+                if (flag == 1) fB = phi(i, k);
+                if (flag == 3) fB = phi(c.No_cp(nc, 3), k);
+                if (flag != -1) phi(nc, k) = fB;
+            }
+}
+
+// interpolation2D (interpolation2D.F90:120-135) for all layers, then the
+// vertical placement of interpolation3D/3DP (interpolation3D.F90:151-198,
+// 379-423).
+void interpolation3D(orc_ctx& c, R2& phiv, const R2& phi, int tagdir) {
+    const int NV = c.NV, NZ = c.NZ;
+    if (tagdir == 2) {
+#pragma omp parallel for schedule(static)
+        for (int k = 1; k <= NZ - 1; ++k)
+            for (int nv = 1; nv <= NV; ++nv) {
+                double s = 0.0;
+                for (int j = 1; j <= c.Dimsurrounding(nv); ++j)
+                    s = s + c.weight(nv, j) * phi(c.surrounding(nv, j), k);
+                phiv(nv, k) = s / c.dlVsum(nv);
+            }
+    } else {
+        R2 dz0; dz0.init(NV, NZ);
+#pragma omp parallel for schedule(static)
+        for (int k = 1; k <= NZ; ++k)
+            for (int nv = 1; nv <= NV; ++nv) {
+                double s = 0.0;
+                for (int j = 1; j <= c.Dimsurrounding(nv); ++j)
+                    s = s + c.weight(nv, j) * phi(c.surrounding(nv, j), k);
+                dz0(nv, k) = s / c.dlVsum(nv);
+            }
+#pragma omp parallel for schedule(static)
+        for (int k = 1; k <= NZ - 1; ++k) {
+            double dzT = std::fabs(c.sigv(k) - c.sig(k + 1));
+            double dzB = std::fabs(c.sigv(k) - c.sig(k));
+            for (int nv = 1; nv <= NV; ++nv)
+                phiv(nv, k) = (dzB * dz0(nv, k + 1) + dzT * dz0(nv, k)) / (dzT + dzB);
+        }
+    }
+}
+
+// bc_periodic, serial branch: BC.F90:1243-1300
+void bc_periodic(orc_ctx& c, R2& phiv, int tagBC) {
+    const int NV = c.NV, NZ = c.NZ;
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= NZ - 1; ++k) {
+        std::vector<double> old(NV + 1, 0.0);
+        for (int nv : c.bnd_verts) {
+            if (c.vertex_edge(nv) == 1) {
+                double sumdlV = 0.0;
+                for (int pair : c.corner_list) {
+                    old[nv] = old[nv] + phiv(pair, k) * c.dlVsum(pair);
+                    sumdlV = sumdlV + c.dlVsum(pair);
+                }
+                old[nv] = old[nv] / sumdlV;
+            } else if (c.vertex_pair(nv) > 0) {
+                int pair = c.vertex_pair(nv);
+                double sumdlV = c.dlVsum(nv) + c.dlVsum(pair);
+                old[nv] = c.dlVsum(nv) * phiv(nv, k) + c.dlVsum(pair) * phiv(pair, k);
+                old[nv] = old[nv] / sumdlV;
+            }
+        }
+        for (int nv : c.bnd_verts) {
+            int flag = (tagBC == TagBCu) ? c.bcuv(nv) : (tagBC == TagBCv) ? c.bcvv(nv)
+                     : (tagBC == TagBCw) ? c.bcwv(nv) : c.bcpv(nv);
+            if (flag == 3) phiv(nv, k) = old[nv];
+        }
+    }
+}
+
+// BCvelvertex3D: BC.F90:603-807
+void BCvelvertex3D(orc_ctx& c, R2& phiv, int tagBC, int tagdir) {
+    const int NV = c.NV, NZ = c.NZ;
+    for (int nv : c.bnd_verts) {
+        int flag = (tagBC == 1) ? c.bcuv(nv) : (tagBC == 2) ? c.bcvv(nv) : c.bcwv(nv);
+        if (flag == 0)
+            for (int k = 1; k <= NZ - 1; ++k) phiv(nv, k) = 0.;
+    }
+    if (tagdir == 3) {
+        if (c.bcbot == 1 && (c.P.bot_bc == 0 || tagBC == 3))
+            for (int nv = 1; nv <= NV; ++nv) phiv(nv, 1) = 0.;
+        if (c.bctop == 1 && (c.P.top_bc == 0 || tagBC == 3))
+            for (int nv = 1; nv <= NV; ++nv) phiv(nv, NZ - 1) = 0.;
+    }
+    bc_periodic(c, phiv, tagBC);
+}
+
+// BCpvertex: BC.F90:986-1135
+void BCpvertex(orc_ctx& c, R2& phiv) {
+    for (int nv : c.bnd_verts)
+        if (c.bcpv(nv) == 0)
+            for (int k = 1; k <= c.NZ - 1; ++k) phiv(nv, k) = 0.;
+    bc_periodic(c, phiv, TagBCp);
+}
+
+// BCglobalVC: BC.F90:202-295
+void BCglobalVC(orc_ctx& c, R2& u, R2& v, R2& w, R2& uv, R2& vv, R2& wv, int tagdir) {
+    BCvelcenter3D(c, u, TagBCu); interpolation3D(c, uv, u, tagdir); BCvelvertex3D(c, uv, TagBCu, tagdir);
+    BCvelcenter3D(c, v, TagBCv); interpolation3D(c, vv, v, tagdir); BCvelvertex3D(c, vv, TagBCv, tagdir);
+    BCvelcenter3D(c, w, TagBCw); interpolation3D(c, wv, w, tagdir); BCvelvertex3D(c, wv, TagBCw, tagdir);
+}
+
+// BCglobalP: BC.F90:299-363
+void BCglobalP(orc_ctx& c, R2& p, R2& pv, int tagdir) {
+    BCpcenter(c, p);
+    interpolation3D(c, pv, p, tagdir);
+    BCpvertex(c, pv);
+}
+
+// ---------------------------------------------------------------------------
+// Operators
+// ---------------------------------------------------------------------------
+
+// grandientLSM: gradientLSM.F90:145-201
+void grandientLSM(orc_ctx& c, R2& dfdx, R2& dfdy, R2& dfds, const R2& fun) {
+    const int N0 = c.N0, NZ = c.NZ, NC = c.NC;
+    std::fill(dfdx.d.begin(), dfdx.d.end(), 0.0);
+    std::fill(dfdy.d.begin(), dfdy.d.end(), 0.0);
+    std::fill(dfds.d.begin(), dfds.d.end(), 0.0);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k) {
+        for (int i = 1; i <= N0; ++i) {
+            double sumfx = 0.0, sumfy = 0.0;
+            for (int j = 1; j <= 3; ++j) {
+                int jc = c.No_cp(i, j);
+                sumfx = sumfx + c.dxCC(i, j) * (fun(jc, k) - fun(i, k));
+                sumfy = sumfy + c.dyCC(i, j) * (fun(jc, k) - fun(i, k));
+            }
+            double deter = c.sum_xc2(i) * c.sum_yc2(i) - c.sum_xcyc(i) * c.sum_xcyc(i);
+            dfdx(i, k) = (c.sum_yc2(i) * sumfx - c.sum_xcyc(i) * sumfy) / deter;
+            dfdy(i, k) = (c.sum_xc2(i) * sumfy - c.sum_xcyc(i) * sumfx) / deter;
+        }
+        double dzp = c.sig(k + 1) - c.sig(k);
+        double dzm = c.sig(k - 1) - c.sig(k);
+        double sumsigsig = dzp * dzp + dzm * dzm;
+        for (int i = 1; i <= NC; ++i)
+            dfds(i, k) = ((fun(i, k + 1) - fun(i, k)) * dzp + (fun(i, k - 1) - fun(i, k)) * dzm) / sumsigsig;
+    }
+    BCpcenter(c, dfdx);
+    BCpcenter(c, dfdy);
+    BCpcenter(c, dfds);
+}
+
+// calcul_face, KeyKimChoi branch: interpolationFace.F90:85-111
+void calcul_face(orc_ctx& c, R2& f1, R2& f2, R2& f3, R2& fT, R2& fB, const R2& fun, const R2& funv) {
+    const int N0 = c.N0, NZ = c.NZ;
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            double phi[4];
+            for (int j = 1; j <= 3; ++j) {
+                int jc = c.No_cp(i, j);
+                int jj = j + 1; if (jj > 3) jj -= 3;
+                int nv1 = c.No_vp(i, j), nv2 = c.No_vp(i, jj);
+                double phi1 = fun(i, k), phi2 = fun(jc, k);
+                double extra = c.doe(i, j) * (funv(nv2, k) - funv(nv1, k)) / c.dlVV(i, j);
+                phi[j] = phi2 * 0.5 + phi1 * 0.5 + extra;
+            }
+            f1(i, k) = phi[1]; f2(i, k) = phi[2]; f3(i, k) = phi[3];
+            fT(i, k) = 0.5 * (fun(i, k) + fun(i, k + 1));
+            fB(i, k) = 0.5 * (fun(i, k) + fun(i, k - 1));
+        }
+}
+
+// diffusion3DNEW, KeyKimChoi branch: diffusion3D.F90:95-191
+void diffusion3DNEW(orc_ctx& c, R2& rhsu, R2& rhsv, R2& rhsw, const R2& pu, const R2& pv,
+                    const R2& pw, const R2& puv, const R2& pvv, const R2& pwv,
+                    const R2& Gx, const R2& Gy, const R2& Gz) {
+    const int N0 = c.N0, NZ = c.NZ, NC = c.NC;
+    R2 dudx, dudy, duds, dvdx, dvdy, dvds, dwdx, dwdy, dwds;
+    dudx.init(NC, NZ); dudy.init(NC, NZ); duds.init(NC, NZ);
+    dvdx.init(NC, NZ); dvdy.init(NC, NZ); dvds.init(NC, NZ);
+    dwdx.init(NC, NZ); dwdy.init(NC, NZ); dwds.init(NC, NZ);
+    // The reference computes these three LSQ gradients and then multiplies
+    // their contribution by dle3 = 0 (calcul_geometry.F90:1493).  The work is
+    // kept so that the CPU baseline does what the reference does.
+    grandientLSM(c, dudx, dudy, duds, pu);
+    grandientLSM(c, dvdx, dvdy, dvds, pv);
+    grandientLSM(c, dwdx, dwdy, dwds, pw);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            double Vol = c.areaCell(i) * c.dsigv(k - 1);
+            double dudn[4], dvdn[4], dwdn[4];
+            for (int j = 1; j <= 3; ++j) {
+                int jc = c.No_cp(i, j);
+                int jj = j + 1; if (jj > 3) jj -= 3;
+                int jv1 = c.No_vp(i, j), jv2 = c.No_vp(i, jj);
+                double co1 = c.dle1(i, j), co2 = c.dle2(i, j), co3 = c.dle3(i, j);
+                double dxm = c.xmo(i, j) - c.xme(i, j), dym = c.ymo(i, j) - c.yme(i, j);
+                double diff1 = (pu(jc, k) - pu(i, k)) / c.dlCC(i, j);
+                double diff2 = (puv(jv2, k) - puv(jv1, k)) / c.dlVV(i, j);
+                double diff3 = dxm * (dudx(jc, k) - dudx(i, k)) + dym * (dudy(jc, k) - dudy(i, k));
+                dudn[j] = diff1 * co1 + diff2 * co2 + diff3 * co3;
+                diff1 = (pv(jc, k) - pv(i, k)) / c.dlCC(i, j);
+                diff2 = (pvv(jv2, k) - pvv(jv1, k)) / c.dlVV(i, j);
+                diff3 = dxm * (dvdx(jc, k) - dvdx(i, k)) + dym * (dvdy(jc, k) - dvdy(i, k));
+                dvdn[j] = diff1 * co1 + diff2 * co2 + diff3 * co3;
+                diff1 = (pw(jc, k) - pw(i, k)) / c.dlCC(i, j);
+                diff2 = (pwv(jv2, k) - pwv(jv1, k)) / c.dlVV(i, j);
+                diff3 = dxm * (dwdx(jc, k) - dwdx(i, k)) + dym * (dwdy(jc, k) - dwdy(i, k));
+                dwdn[j] = diff1 * co1 + diff2 * co2 + diff3 * co3;
+            }
+            double dudT = (pu(i, k + 1) - pu(i, k)) / c.dsig(k);
+            double dudB = (pu(i, k - 1) - pu(i, k)) / c.dsig(k - 1);
+            double dvdT = (pv(i, k + 1) - pv(i, k)) / c.dsig(k);
+            double dvdB = (pv(i, k - 1) - pv(i, k)) / c.dsig(k - 1);
+            double dwdT = (pw(i, k + 1) - pw(i, k)) / c.dsig(k);
+            double dwdB = (pw(i, k - 1) - pw(i, k)) / c.dsig(k - 1);
+            double dsv = c.dsigv(k - 1);
+            double su = dudn[1] * c.dlVV(i, 1) * dsv + dudn[2] * c.dlVV(i, 2) * dsv +
+                        dudn[3] * c.dlVV(i, 3) * dsv + (dudT + dudB) * c.areaCell(i);
+            double sv = dvdn[1] * c.dlVV(i, 1) * dsv + dvdn[2] * c.dlVV(i, 2) * dsv +
+                        dvdn[3] * c.dlVV(i, 3) * dsv + (dvdT + dvdB) * c.areaCell(i);
+            double sw = dwdn[1] * c.dlVV(i, 1) * dsv + dwdn[2] * c.dlVV(i, 2) * dsv +
+                        dwdn[3] * c.dlVV(i, 3) * dsv + (dwdT + dwdB) * c.areaCell(i);
+            rhsu(i, k) = rhsu(i, k) + Gx(i, k) * su / Vol;
+            rhsv(i, k) = rhsv(i, k) + Gy(i, k) * sv / Vol;
+            rhsw(i, k) = rhsw(i, k) + Gz(i, k) * sw / Vol;
+        }
+}
+
+// advection3DNEW: advection3D.F90:96-302 (explicit, no KeyImplicit)
+void advection3DNEW(orc_ctx& c, R2& rhsu, R2& rhsv, R2& rhsw, const R2& pu, const R2& pv,
+                    const R2& pw, const R2& puv, const R2& pvv, const R2& pwv) {
+    const int N0 = c.N0, NZ = c.NZ;
+    R2 Ui1, Ui2, Ui3, UiT, UiB, Vi1, Vi2, Vi3, ViT, ViB, Wi1, Wi2, Wi3, WiT, WiB;
+    for (R2* a : {&Ui1, &Ui2, &Ui3, &UiT, &UiB, &Vi1, &Vi2, &Vi3, &ViT, &ViB, &Wi1, &Wi2, &Wi3, &WiT, &WiB})
+        a->init(N0, NZ);
+    calcul_face(c, Ui1, Ui2, Ui3, UiT, UiB, pu, puv);
+    calcul_face(c, Vi1, Vi2, Vi3, ViT, ViB, pv, pvv);
+    calcul_face(c, Wi1, Wi2, Wi3, WiT, WiB, pw, pwv);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            double dsv = c.dsigv(k - 1);
+            double F1 = c.U1FACE(i, k) * c.dlVV(i, 1) * dsv;
+            double F2 = c.U2FACE(i, k) * c.dlVV(i, 2) * dsv;
+            double F3 = c.U3FACE(i, k) * c.dlVV(i, 3) * dsv;
+            double FT = c.UTFACE(i, k) * c.areaCell(i);
+            double FB = c.UBFACE(i, k) * c.areaCell(i);
+            double uflux = Ui1(i, k) * F1 + Ui2(i, k) * F2 + Ui3(i, k) * F3 + UiT(i, k) * FT + UiB(i, k) * FB;
+            double vflux = Vi1(i, k) * F1 + Vi2(i, k) * F2 + Vi3(i, k) * F3 + ViT(i, k) * FT + ViB(i, k) * FB;
+            double wflux = Wi1(i, k) * F1 + Wi2(i, k) * F2 + Wi3(i, k) * F3 + WiT(i, k) * FT + WiB(i, k) * FB;
+            double Vol = c.areaCell(i) * dsv;
+            rhsu(i, k) = rhsu(i, k) - uflux / Vol;
+            rhsv(i, k) = rhsv(i, k) - vflux / Vol;
+            rhsw(i, k) = rhsw(i, k) - wflux / Vol;
+        }
+}
+
+// AdvDiffNS: AdvDiffNS.F90:77-132
+void AdvDiffNS(orc_ctx& c, R2& rhsu, R2& rhsv, R2& rhsw, R2& u, R2& v, R2& w,
+               const R2& Gx, const R2& Gy, const R2& Gz) {
+    R2 uv, vv, wv;
+    uv.init(c.NV, c.NZ - 1); vv.init(c.NV, c.NZ - 1); wv.init(c.NV, c.NZ - 1);
+    BCglobalVC(c, u, v, w, uv, vv, wv, 2);
+    diffusion3DNEW(c, rhsu, rhsv, rhsw, u, v, w, uv, vv, wv, Gx, Gy, Gz);
+    advection3DNEW(c, rhsu, rhsv, rhsw, u, v, w, uv, vv, wv);
+}
+
+// sgdamp: sgm_les.F90:1247-1281
+void sgdamp(double& del, double dist, double yplus, bool van) {
+    if (!van) {
+        double lwall = von_Karman * dist;
+        double n = sg_smag_mason;
+        double dn1 = std::pow(1.0 / del, n) + std::pow(1.0 / lwall, n);
+        double dn2 = 1.0 / dn1;
+        del = std::pow(dn2, 1.0 / n);
+    } else {
+        double lwall = von_Karman * dist;
+        if (lwall > del) lwall = del;
+        del = lwall * (1.0 - std::exp(-yplus / sg_smag_aplus));
+    }
+    del = del * del;
+}
+
+// fvm_gradient: sgm_les.F90:284-502
+void fvm_gradient(orc_ctx& c, R2& u, R2& v, R2& w, R2 g[9]) {
+    const int N0 = c.N0, NZ = c.NZ;
+    R2 uv, vv, wv;
+    uv.init(c.NV, NZ - 1); vv.init(c.NV, NZ - 1); wv.init(c.NV, NZ - 1);
+    BCglobalVC(c, u, v, w, uv, vv, wv, 2);
+    R2 Ui1, Ui2, Ui3, UiT, UiB, Vi1, Vi2, Vi3, ViT, ViB, Wi1, Wi2, Wi3, WiT, WiB;
+    for (R2* a : {&Ui1, &Ui2, &Ui3, &UiT, &UiB, &Vi1, &Vi2, &Vi3, &ViT, &ViB, &Wi1, &Wi2, &Wi3, &WiT, &WiB})
+        a->init(N0, NZ);
+    calcul_face(c, Ui1, Ui2, Ui3, UiT, UiB, u, uv);
+    calcul_face(c, Vi1, Vi2, Vi3, ViT, ViB, v, vv);
+    calcul_face(c, Wi1, Wi2, Wi3, WiT, WiB, w, wv);
+    const bool compat = c.P.ref_bug_compat != 0;
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            // Reference quirk (sgm_les.F90:445-446, 454-455): the v gradient
+            // pairs face 2 with dlVV(i,3) and face 3 with dlVV(i,2).
+            int l2 = compat ? 3 : 2, l3 = compat ? 2 : 3;
+            double a = c.areaCell(i);
+            double dudx = Ui1(i, k) * c.xnn(i, 1) * c.dlVV(i, 1) + Ui2(i, k) * c.xnn(i, 2) * c.dlVV(i, 2) +
+                          Ui3(i, k) * c.xnn(i, 3) * c.dlVV(i, 3);
+            double dvdx = Vi1(i, k) * c.xnn(i, 1) * c.dlVV(i, 1) + Vi2(i, k) * c.xnn(i, 2) * c.dlVV(i, l2) +
+                          Vi3(i, k) * c.xnn(i, 3) * c.dlVV(i, l3);
+            double dwdx = Wi1(i, k) * c.xnn(i, 1) * c.dlVV(i, 1) + Wi2(i, k) * c.xnn(i, 2) * c.dlVV(i, 2) +
+                          Wi3(i, k) * c.xnn(i, 3) * c.dlVV(i, 3);
+            double dudy = Ui1(i, k) * c.ynn(i, 1) * c.dlVV(i, 1) + Ui2(i, k) * c.ynn(i, 2) * c.dlVV(i, 2) +
+                          Ui3(i, k) * c.ynn(i, 3) * c.dlVV(i, 3);
+            double dvdy = Vi1(i, k) * c.ynn(i, 1) * c.dlVV(i, 1) + Vi2(i, k) * c.ynn(i, 2) * c.dlVV(i, l2) +
+                          Vi3(i, k) * c.ynn(i, 3) * c.dlVV(i, l3);
+            double dwdy = Wi1(i, k) * c.ynn(i, 1) * c.dlVV(i, 1) + Wi2(i, k) * c.ynn(i, 2) * c.dlVV(i, 2) +
+                          Wi3(i, k) * c.ynn(i, 3) * c.dlVV(i, 3);
+            g[0](i, k) = dudx / a; g[3](i, k) = dvdx / a; g[6](i, k) = dwdx / a;
+            g[1](i, k) = dudy / a; g[4](i, k) = dvdy / a; g[7](i, k) = dwdy / a;
+            double hz = compat ? c.dsig(k) : c.dsigv(k - 1);
+            g[2](i, k) = (UiT(i, k) - UiB(i, k)) / hz;
+            g[5](i, k) = (ViT(i, k) - ViB(i, k)) / hz;
+            g[8](i, k) = (WiT(i, k) - WiB(i, k)) / hz;
+        }
+}
+
+// sgles: sgm_les.F90:24-275 with KeyTESTChannel (u_tau = 1) and the wall
+// distance of sgmkwd (sgm_les.F90:856-862).
+void sgles(orc_ctx& c, R2& u, R2& v, R2& w) {
+    const int N0 = c.N0, NZ = c.NZ, NC = c.NC;
+    const orc_params& P = c.P;
+    if (c.sg_init == 1) {
+        c.walld.init(NC, NZ, 1.0E5);
+        c.eddy.init(NC, NZ, 0.0);
+        for (int k = 1; k <= NZ; ++k)
+            for (int i = 1; i <= NC; ++i) {
+                double z = c.sig(k);
+                double d = std::fabs(z);  // reference: distance to the bottom wall only
+                if (P.ref_bug_compat == 0) {
+                    d = std::fabs(z - P.sigini);
+                    if (P.top_bc == 0) d = std::min(d, std::fabs(P.sigfin - z));
+                }
+                c.walld(i, k) = d;
+            }
+        c.sg_init = 0;
+    }
+    R2 g[9];
+    for (int q = 0; q < 9; ++q) g[q].init(NC, NZ);
+    fvm_gradient(c, u, v, w, g);
+    const double Cs = sg_smag_const;
+    const bool van = P.les_van != 0;
+    double maxeddy = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : maxeddy)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            const double Hpr = 1.0;  // user_initial.F90:159
+            double DD = Cs * std::pow(c.areaCell(i) * c.dsig(k) * Hpr, 1.0 / 3.0);
+            double dist = c.walld(i, k);
+            double lwplus = van ? dist * 1.0 * P.re : 0.0;
+            sgdamp(DD, dist, lwplus, van);
+            double Sdudx = g[0](i, k), Sdudy = g[1](i, k), Sdudz = g[2](i, k);
+            double Sdvdx = g[3](i, k), Sdvdy = g[4](i, k), Sdvdz = g[5](i, k);
+            double Sdwdx = g[6](i, k), Sdwdy = g[7](i, k), Sdwdz = g[8](i, k);
+            double nut = Hpr * DD;
+            double sxx = (Sdudx + Sdudx) / 2.0;
+            double sxy = (Sdudy + Sdvdx) / 2.0;
+            double sxz = (Sdudz + Sdwdx) / 2.0;
+            double syy = (Sdvdy + Sdvdy) / 2.0;
+            double syz = (Sdvdz + Sdwdy) / 2.0;
+            double szz = (Sdwdz + Sdwdz) / 2.0;
+            double Sij = std::sqrt(2.0 * (sxx * sxx + syy * syy + szz * szz) +
+                                   4.0 * (sxy * sxy + sxz * sxz + syz * syz));
+            c.eddy(i, k) = nut * Sij;
+            if (c.eddy(i, k) > maxeddy) maxeddy = c.eddy(i, k);
+        }
+    BCpcenter(c, c.eddy);
+    c.info.max_eddy = maxeddy;
+}
+
+// interpolateU: interpolationU.F90:99-160 (writes the face fluxes)
+void interpolateU(orc_ctx& c, R2& u, R2& v, R2& w) {
+    const int N0 = c.N0, NZ = c.NZ;
+    R2 uv, vv, wv;
+    uv.init(c.NV, NZ - 1); vv.init(c.NV, NZ - 1); wv.init(c.NV, NZ - 1);
+    // Vertex values are computed and discarded, as in the reference.
+    BCglobalVC(c, u, v, w, uv, vv, wv, 2);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            int jc1 = c.No_cp(i, 1), jc2 = c.No_cp(i, 2), jc3 = c.No_cp(i, 3);
+            double Ui1 = 0.5 * (u(i, k) + u(jc1, k)), Ui2 = 0.5 * (u(i, k) + u(jc2, k)),
+                   Ui3 = 0.5 * (u(i, k) + u(jc3, k));
+            double Vi1 = 0.5 * (v(i, k) + v(jc1, k)), Vi2 = 0.5 * (v(i, k) + v(jc2, k)),
+                   Vi3 = 0.5 * (v(i, k) + v(jc3, k));
+            double WiT = 0.5 * (w(i, k) + w(i, k + 1)), WiB = 0.5 * (w(i, k) + w(i, k - 1));
+            c.U1FACE(i, k) = Ui1 * c.xnn(i, 1) + Vi1 * c.ynn(i, 1);
+            c.U2FACE(i, k) = Ui2 * c.xnn(i, 2) + Vi2 * c.ynn(i, 2);
+            c.U3FACE(i, k) = Ui3 * c.xnn(i, 3) + Vi3 * c.ynn(i, 3);
+            c.UTFACE(i, k) = WiT;
+            c.UBFACE(i, k) = -1.0 * WiB;
+        }
+}
+
+// Source3D, Option 1: source3D.F90:92-127
+void source3D(orc_ctx& c, R2& rhsp, R2& u, R2& v, R2& w) {
+    const int N0 = c.N0, NZ = c.NZ;
+    interpolateU(c, u, v, w);
+    std::fill(rhsp.d.begin(), rhsp.d.end(), 0.0);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            double resid = 0.0;
+            double dsv = c.dsigv(k - 1);
+            resid = resid + c.U1FACE(i, k) * c.dlVV(i, 1) * dsv;
+            resid = resid + c.U2FACE(i, k) * c.dlVV(i, 2) * dsv;
+            resid = resid + c.U3FACE(i, k) * c.dlVV(i, 3) * dsv;
+            resid = resid + c.UTFACE(i, k) * c.areaCell(i);
+            resid = resid + c.UBFACE(i, k) * c.areaCell(i);
+            rhsp(i, k) = resid;
+        }
+}
+
+// update_rhsp, KeyKimChoi branch: source3D.F90:255-288
+void update_rhsp(orc_ctx& c, R2& rhs, R2& phi, R2& phiv, const R2& dpdx, const R2& dpdy) {
+    const int N0 = c.N0, NZ = c.NZ;
+    BCglobalP(c, phi, phiv, 2);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            double dn[4];
+            for (int j = 1; j <= 3; ++j) {
+                int jc = c.No_cp(i, j);
+                int jj = j + 1; if (jj > 3) jj -= 3;
+                int jv1 = c.No_vp(i, j), jv2 = c.No_vp(i, jj);
+                double diff2 = (phiv(jv2, k) - phiv(jv1, k)) / c.dlVV(i, j);
+                double diff3 = (c.xmo(i, j) - c.xme(i, j)) * (dpdx(jc, k) - dpdx(i, k)) +
+                               (c.ymo(i, j) - c.yme(i, j)) * (dpdy(jc, k) - dpdy(i, k));
+                dn[j] = diff2 * c.dle2(i, j) + diff3 * c.dle3(i, j);
+            }
+            double dsv = c.dsigv(k - 1);
+            double source = dn[1] * c.dlVV(i, 1) * dsv + dn[2] * c.dlVV(i, 2) * dsv + dn[3] * c.dlVV(i, 3) * dsv;
+            rhs(i, k) = rhs(i, k) - source;
+        }
+}
+
+// Glob_Norm: bicgstab.F90:598-666
+void Glob_Norm(orc_ctx& c, R2& field, int tags) {
+    const int N0 = c.N0, NZ = c.NZ;
+    const bool compat = c.P.ref_bug_compat != 0;
+    // Reference quirk: the layer weight is dsig(k) (cell-centre spacing)
+    // where the cell height is dsigv(k-1); the two agree on a uniform grid.
+    auto h = [&](int k) { return compat ? c.dsig(k) : c.dsigv(k - 1); };
+    double glob_sum = ksum(2, NZ - 1, [&](int k) {
+        double s = 0.0;
+        for (int i = 1; i <= N0; ++i) {
+            double Vol = c.areaCell(i) * h(k);
+            if (tags == 1) s = field(i, k) + s;
+            else s = field(i, k) * Vol + s;
+        }
+        return s;
+    });
+    double avec = glob_sum / (c.TotalVolume * c.Lsig);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            if (tags == 1) field(i, k) = field(i, k) - avec * c.areaCell(i) * h(k);
+            else field(i, k) = field(i, k) - avec;
+        }
+}
+
+struct Krylov {
+    R2 r0bar, vk, sk, tk, yk, rk, pk, zk;
+};
+
+// get_Apk (bicgstab.F90:931-1001) with BCpcenter on the input vector.
+void get_Apk(orc_ctx& c, R2& out, R2& in) {
+    const int N0 = c.N0, NZ = c.NZ;
+    BCpcenter(c, in);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            int jc1 = c.No_cp(i, 1), jc2 = c.No_cp(i, 2), jc3 = c.No_cp(i, 3);
+            double rsum = c.AmC0(i, k) * in(i, k) + c.AmC1(i, k) * in(jc1, k) + c.AmC2(i, k) * in(jc2, k) +
+                          c.AmC3(i, k) * in(jc3, k) + c.AmCT(i, k) * in(i, k + 1) + c.AmCB(i, k) * in(i, k - 1);
+            out(i, k) = rsum;
+        }
+}
+
+double innerprod(orc_ctx& c, const R2& a, const R2& b) {
+    return ksum(2, c.NZ - 1, [&](int k) {
+        double s = 0.0;
+        for (int i = 1; i <= c.N0; ++i) s = s + a(i, k) * b(i, k);
+        return s;
+    });
+}
+
+// BICGSTAB_SOLVE: bicgstab.F90:303-591 (Jacobi preconditioner, Opt = 1)
+void BICGSTAB_SOLVE(orc_ctx& c, R2& rhs, R2& phi) {
+    const int N0 = c.N0, NZ = c.NZ, NC = c.NC;
+    Krylov K;
+    for (R2* a : {&K.r0bar, &K.vk, &K.sk, &K.tk, &K.yk, &K.rk, &K.pk, &K.zk}) a->init(NC, NZ);
+    // initial residual and norms
+    std::vector<double> pb2(NZ + 1), pr2(NZ + 1), pb1(NZ + 1), pr1(NZ + 1);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k) {
+        double b2 = 0, r2 = 0, b1 = 0, r1 = 0;
+        for (int i = 1; i <= N0; ++i) {
+            int jc1 = c.No_cp(i, 1), jc2 = c.No_cp(i, 2), jc3 = c.No_cp(i, 3);
+            double resid = rhs(i, k) - (c.AmC0(i, k) * phi(i, k) + c.AmC1(i, k) * phi(jc1, k) +
+                                        c.AmC2(i, k) * phi(jc2, k) + c.AmC3(i, k) * phi(jc3, k) +
+                                        c.AmCT(i, k) * phi(i, k + 1) + c.AmCB(i, k) * phi(i, k - 1));
+            b2 = b2 + rhs(i, k) * rhs(i, k);
+            r2 = r2 + resid * resid;
+            b1 = b1 + std::fabs(rhs(i, k));
+            r1 = r1 + std::fabs(resid);
+            K.rk(i, k) = resid;
+            K.r0bar(i, k) = resid;
+        }
+        pb2[k] = b2; pr2[k] = r2; pb1[k] = b1; pr1[k] = r1;
+    }
+    double b2norm = 0, r2norm = 0, b1norm = 0, r1norm = 0;
+    for (int k = 2; k <= NZ - 1; ++k) { b2norm += pb2[k]; r2norm += pr2[k]; b1norm += pb1[k]; r1norm += pr1[k]; }
+    b2norm = std::sqrt(b2norm);
+    r2norm = std::sqrt(r2norm);
+    if (b2norm == 0) b2norm = 1.0;
+    if (b1norm == 0) b1norm = 1.0;
+    double e2norm = r2norm / b2norm, e1norm = r1norm / b1norm;
+    c.info.iters = 0; c.info.e1norm = e1norm; c.info.e2norm = e2norm; c.info.converged = 1;
+    if (e1norm < c.P.eps || e2norm < c.P.eps) return;  // converged without solve
+    double rhokm = 1.0, alpha = 1.0, omegakm = 1.0;
+    int iter = 0;
+    c.info.converged = 0;
+    for (;;) {
+        if (std::fabs(rhokm) < 1.0e-30) break;
+        if (std::fabs(omegakm) < 1.0e-30) break;
+        double rhok = innerprod(c, K.r0bar, K.rk);
+        // update_pk: bicgstab.F90:726-773
+        if (iter == 0) {
+#pragma omp parallel for schedule(static)
+            for (int k = 2; k <= NZ - 1; ++k)
+                for (int i = 1; i <= N0; ++i) K.pk(i, k) = K.rk(i, k);
+        } else {
+            double beta = (rhok / rhokm) * (alpha / omegakm);
+#pragma omp parallel for schedule(static)
+            for (int k = 2; k <= NZ - 1; ++k)
+                for (int i = 1; i <= N0; ++i) K.pk(i, k) = K.rk(i, k) + beta * (K.pk(i, k) - omegakm * K.vk(i, k));
+        }
+        // diag_precdt: bicgstab.F90:779-925 (Opt = 1)
+#pragma omp parallel for schedule(static)
+        for (int k = 2; k <= NZ - 1; ++k)
+            for (int i = 1; i <= N0; ++i) K.yk(i, k) = K.pk(i, k) / c.AmC0(i, k);
+        get_Apk(c, K.vk, K.yk);
+        double r0barvk = innerprod(c, K.r0bar, K.vk);
+        if (std::fabs(r0barvk) < 1.0e-30) break;
+        alpha = rhok / r0barvk;
+        // update_sk
+#pragma omp parallel for schedule(static)
+        for (int k = 2; k <= NZ - 1; ++k)
+            for (int i = 1; i <= N0; ++i) K.sk(i, k) = K.rk(i, k) - alpha * K.vk(i, k);
+#pragma omp parallel for schedule(static)
+        for (int k = 2; k <= NZ - 1; ++k)
+            for (int i = 1; i <= N0; ++i) K.zk(i, k) = K.sk(i, k) / c.AmC0(i, k);
+        get_Apk(c, K.tk, K.zk);
+        double var1 = innerprod(c, K.tk, K.sk);
+        double var2 = innerprod(c, K.tk, K.tk);
+        omegakm = var1 / var2;
+        // update_xkrk: bicgstab.F90:1047-1111
+        std::vector<double> q1(NZ + 1), q2(NZ + 1);
+#pragma omp parallel for schedule(static)
+        for (int k = 2; k <= NZ - 1; ++k) {
+            double s1 = 0, s2 = 0;
+            for (int i = 1; i <= N0; ++i) {
+                double xnew = phi(i, k) + alpha * K.yk(i, k) + omegakm * K.zk(i, k);
+                double resid = K.sk(i, k) - omegakm * K.tk(i, k);
+                s2 = s2 + resid * resid;
+                s1 = s1 + std::fabs(resid);
+                phi(i, k) = xnew;
+                K.rk(i, k) = resid;
+            }
+            q1[k] = s1; q2[k] = s2;
+        }
+        double sr1 = 0, sr2 = 0;
+        for (int k = 2; k <= NZ - 1; ++k) { sr1 += q1[k]; sr2 += q2[k]; }
+        r2norm = std::sqrt(sr2);
+        r1norm = sr1;
+        e2norm = r2norm / b2norm;
+        e1norm = r1norm / b1norm;
+        rhokm = rhok;
+        iter = iter + 1;
+        double enorm = 1.0E10;
+        if (enorm > e1norm) enorm = e1norm;
+        if (enorm > e2norm) enorm = e2norm;
+        c.info.iters = iter; c.info.e1norm = e1norm; c.info.e2norm = e2norm;
+        if (enorm < c.P.eps) { c.info.converged = 1; break; }
+        if (iter > c.P.max_iters) break;
+    }
+}
+
+// bicgstab: bicgstab.F90:95-168 (KeyTESTChannel: flg = 1)
+void bicgstab(orc_ctx& c, R2& phi, R2& phiv, R2& rhs) {
+    Glob_Norm(c, rhs, 1);
+    BICGSTAB_SOLVE(c, rhs, phi);
+    Glob_Norm(c, phi, 0);
+    BCglobalP(c, phi, phiv, 3);
+}
+
+// gradientP (gradientP.F90:79-83): Option 2 -> grandientLSM
+void gradientP(orc_ctx& c, R2& fun, R2& dx, R2& dy, R2& ds) { grandientLSM(c, dx, dy, ds, fun); }
+
+// newu3D, KeyKimChoi branch: newu3D.F90:109-239
+void newu3D(orc_ctx& c, R2& fun, R2& funv, const R2& dpdx, const R2& dpdy) {
+    const int N0 = c.N0, NZ = c.NZ;
+    const double c1 = c.P.dt;
+    const bool compat = c.P.ref_bug_compat != 0;
+    BCglobalP(c, fun, funv, 2);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            double dfundn[4];
+            for (int j = 1; j <= 3; ++j) {
+                int jc = c.No_cp(i, j);
+                int jj = j + 1; if (jj > 3) jj -= 3;
+                int jv1 = c.No_vp(i, j), jv2 = c.No_vp(i, jj);
+                double co1 = c.dle1(i, j), co3 = c.dle3(i, j);
+                if (c.bcpc(jc) == 1) { dfundn[j] = 0.; continue; }
+                double co2 = c.dle2(i, j);
+                double diff1 = (fun(jc, k) - fun(i, k)) / c.dlCC(i, j);
+                double diff2 = (funv(jv2, k) - funv(jv1, k)) / c.dlVV(i, j);
+                double diff3 = (c.xmo(i, j) - c.xme(i, j)) * (dpdx(jc, k) - dpdx(i, k)) +
+                               (c.ymo(i, j) - c.yme(i, j)) * (dpdy(jc, k) - dpdy(i, k));
+                dfundn[j] = diff1 * co1 + diff2 * co2 + diff3 * co3;
+            }
+            double dT = (fun(i, k + 1) - fun(i, k)) / c.dsig(k);
+            // Reference quirk (newu3D.F90:164): bottom face divides by dsig(k).
+            double dB = (fun(i, k - 1) - fun(i, k)) / (compat ? c.dsig(k) : c.dsig(k - 1));
+            c.U1FACE(i, k) = c.U1FACE(i, k) - dfundn[1] * c1;
+            c.U2FACE(i, k) = c.U2FACE(i, k) - dfundn[2] * c1;
+            c.U3FACE(i, k) = c.U3FACE(i, k) - dfundn[3] * c1;
+            c.UTFACE(i, k) = c.UTFACE(i, k) - dT * c1;
+            c.UBFACE(i, k) = c.UBFACE(i, k) - dB * c1;
+        }
+}
+
+// hydro: Main/hydro.F90:197-478 (one stage).
+void hydro(orc_ctx& c, int fin_rk) {
+    const int N0 = c.N0, NZ = c.NZ, NC = c.NC;
+    const orc_params& P = c.P;
+    double c1, c2;
+    if (c.flag_ab == 1) { c1 = 1.55; c2 = -0.55; }
+    else { c1 = 1.0; c2 = 0.0; }
+    R2 ufstar, vfstar, wfstar, Gam, rhsu, rhsv, rhsw, rhsp, dpdx, dpdy, dpds;
+    for (R2* a : {&ufstar, &vfstar, &wfstar, &Gam, &rhsu, &rhsv, &rhsw, &rhsp, &dpdx, &dpdy, &dpds})
+        a->init(NC, NZ);
+    c.info.max_eddy = 0.0;
+    if (P.les) sgles(c, c.uf, c.vf, c.wf);
+    const double invRe = 1.0 / P.re;
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= NZ; ++k)
+        for (int i = 1; i <= NC; ++i) {
+            Gam(i, k) = P.les ? c.eddy(i, k) + invRe : invRe;
+            rhsu(i, k) = P.bdx; rhsv(i, k) = P.bdy; rhsw(i, k) = P.bdz;
+        }
+    ufstar = c.uf; vfstar = c.vf; wfstar = c.wf;
+    AdvDiffNS(c, rhsu, rhsv, rhsw, c.uf, c.vf, c.wf, Gam, Gam, Gam);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            ufstar(i, k) = ufstar(i, k) + P.dt * (c1 * rhsu(i, k) + c2 * c.rhsuf(i, k));
+            vfstar(i, k) = vfstar(i, k) + P.dt * (c1 * rhsv(i, k) + c2 * c.rhsvf(i, k));
+            c.rhsuf(i, k) = rhsu(i, k);
+            c.rhsvf(i, k) = rhsv(i, k);
+            wfstar(i, k) = wfstar(i, k) + P.dt * (c1 * rhsw(i, k) + c2 * c.rhswf(i, k));
+            c.rhswf(i, k) = rhsw(i, k);
+        }
+    BCglobalVC(c, ufstar, vfstar, wfstar, c.ufv, c.vfv, c.wfv, 3);
+    source3D(c, rhsp, ufstar, vfstar, wfstar);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) rhsp(i, k) = rhsp(i, k) / P.dt;
+    gradientP(c, c.pf, dpdx, dpdy, dpds);
+    c.pfnp = c.pf;
+    update_rhsp(c, rhsp, c.pf, c.pfv, dpdx, dpdy);
+    bicgstab(c, c.pfnp, c.pfv, rhsp);
+    gradientP(c, c.pfnp, dpdx, dpdy, dpds);
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            c.ufnp(i, k) = ufstar(i, k) - P.dt * dpdx(i, k);
+            c.vfnp(i, k) = vfstar(i, k) - P.dt * dpdy(i, k);
+            c.wfnp(i, k) = wfstar(i, k) - P.dt * dpds(i, k);
+        }
+    BCglobalVC(c, c.ufnp, c.vfnp, c.wfnp, c.ufv, c.vfv, c.wfv, 3);
+    newu3D(c, c.pfnp, c.pfv, dpdx, dpdy);
+    // hydro.F90:469-478 (time_ab2 = 1)
+    if (fin_rk == 1 && c.flag_ab != 1) c.flag_ab = 1;
+}
+
+R2* field_ptr(orc_ctx& c, int f) {
+    switch (f) {
+        case ORC_U: return &c.ufn; case ORC_V: return &c.vfn; case ORC_W: return &c.wfn; case ORC_P: return &c.pfn;
+        case ORC_U1F: return &c.U1FACE; case ORC_U2F: return &c.U2FACE; case ORC_U3F: return &c.U3FACE;
+        case ORC_UTF: return &c.UTFACE; case ORC_UBF: return &c.UBFACE;
+        case ORC_RHSU: return &c.rhsuf; case ORC_RHSV: return &c.rhsvf; case ORC_RHSW: return &c.rhswf;
+        case ORC_EDDY: return &c.eddy;
+        case ORC_UV: return &c.ufv; case ORC_VV: return &c.vfv; case ORC_WV: return &c.wfv; case ORC_PV: return &c.pfv;
+    }
+    return nullptr;
+}
+
+void set_threads(const orc_ctx& c) {
+#ifdef _OPENMP
+    if (c.P.nthreads > 0) omp_set_num_threads(c.P.nthreads);
+#else
+    (void)c;
+#endif
+}
+
+}  // namespace
+
+extern "C" {
+
+orc_ctx* orc_create(const orc_params* prm, const int* No_vp, const int* No_cp, const int* nbe,
+                    const int* nbev, const double* xv, const double* yv, int* err) {
+    if (err) *err = 0;
+    if (!prm || prm->n0 <= 0 || prm->nvert <= 0 || prm->nz < 4) { if (err) *err = -1; return nullptr; }
+    orc_ctx* c = new orc_ctx();
+    c->P = *prm;
+    c->N0 = prm->n0; c->NV = prm->nvert; c->NZ = prm->nz;
+    c->Lsig = prm->sigfin - prm->sigini;
+    set_threads(*c);
+    c->No_vp.init(c->N0, 3); c->No_cp.init(c->N0, 3);
+    c->nbe.init(c->N0); c->nbev.init(c->NV); c->xv.init(c->NV); c->yv.init(c->NV);
+    for (int i = 0; i < 3 * c->N0; ++i) {
+        c->No_vp.d[i] = No_vp[i];
+        c->No_cp.d[i] = No_cp[i];
+        if (No_vp[i] < 1 || No_vp[i] > c->NV || No_cp[i] < 0 || No_cp[i] > c->N0) { delete c; if (err) *err = -2; return nullptr; }
+    }
+    for (int i = 0; i < c->N0; ++i) c->nbe.d[i] = nbe[i];
+    for (int i = 0; i < c->NV; ++i) { c->nbev.d[i] = nbev[i]; c->xv.d[i] = xv[i]; c->yv.d[i] = yv[i]; }
+    int rc = build_geometry(*c);
+    if (rc != 0) { delete c; if (err) *err = rc; return nullptr; }
+    const int NC = c->NC, NZ = c->NZ, N0 = c->N0, NV = c->NV;
+    for (R2* a : {&c->ufn, &c->vfn, &c->wfn, &c->pfn, &c->uf, &c->vf, &c->wf, &c->pf,
+                  &c->ufnp, &c->vfnp, &c->wfnp, &c->pfnp, &c->rhsuf, &c->rhsvf, &c->rhswf})
+        a->init(NC, NZ);
+    for (R2* a : {&c->U1FACE, &c->U2FACE, &c->U3FACE, &c->UTFACE, &c->UBFACE}) a->init(N0, NZ);
+    for (R2* a : {&c->ufv, &c->vfv, &c->wfv, &c->pfv}) a->init(NV, NZ - 1);
+    c->eddy.init(NC, NZ, 0.0);
+    c->walld.init(NC, NZ, 1.0E5);
+    return c;
+}
+
+void orc_destroy(orc_ctx* c) { delete c; }
+int orc_ncell(const orc_ctx* c) { return c->NC; }
+
+int orc_ghost_image(const orc_ctx* c, int* img) {
+    for (int g = c->N0 + 1; g <= c->NC; ++g) img[g - c->N0 - 1] = c->No_cp(g, 3);
+    return c->NC - c->N0;
+}
+
+int orc_no_cp(const orc_ctx* c, int* out) {
+    std::memcpy(out, c->No_cp.d.data(), sizeof(int) * (size_t)c->NC * 3);
+    return 0;
+}
+
+int orc_geom(const orc_ctx* cc, int which, double* out) {
+    orc_ctx& c = const_cast<orc_ctx&>(*cc);
+    const R1* v1 = nullptr;
+    const R2* v2 = nullptr;
+    switch (which) {
+        case ORCG_XC: v1 = &c.xc; break; case ORCG_YC: v1 = &c.yc; break; case ORCG_AREA: v1 = &c.areaCell; break;
+        case ORCG_DLVV: v2 = &c.dlVV; break; case ORCG_DLCC: v2 = &c.dlCC; break;
+        case ORCG_DLE1: v2 = &c.dle1; break; case ORCG_DLE2: v2 = &c.dle2; break; case ORCG_DOE: v2 = &c.doe; break;
+        case ORCG_XNN: v2 = &c.xnn; break; case ORCG_YNN: v2 = &c.ynn; break;
+        case ORCG_DXCC: v2 = &c.dxCC; break; case ORCG_DYCC: v2 = &c.dyCC; break;
+        case ORCG_SUMXC2: v1 = &c.sum_xc2; break; case ORCG_SUMYC2: v1 = &c.sum_yc2; break;
+        case ORCG_SUMXCYC: v1 = &c.sum_xcyc; break;
+        case ORCG_SIG: v1 = &c.sig; break; case ORCG_DSIG: v1 = &c.dsig; break;
+        case ORCG_SIGV: v1 = &c.sigv; break; case ORCG_DSIGV: v1 = &c.dsigv; break;
+        case ORCG_AMC0: v2 = &c.AmC0; break; case ORCG_AMC1: v2 = &c.AmC1; break; case ORCG_AMC2: v2 = &c.AmC2; break;
+        case ORCG_AMC3: v2 = &c.AmC3; break; case ORCG_AMCT: v2 = &c.AmCT; break; case ORCG_AMCB: v2 = &c.AmCB; break;
+        case ORCG_DLVSUM: v1 = &c.dlVsum; break;
+        default: return -1;
+    }
+    if (v1) { std::memcpy(out, v1->d.data(), sizeof(double) * v1->d.size()); return (int)v1->d.size(); }
+    std::memcpy(out, v2->d.data(), sizeof(double) * v2->d.size());
+    return (int)v2->d.size();
+}
+
+int orc_user_initial(orc_ctx* c, const double* u, const double* v, const double* w, const double* p) {
+    set_threads(*c);
+    size_t n = (size_t)c->NC * c->NZ;
+    std::memcpy(c->ufn.d.data(), u, n * sizeof(double));
+    std::memcpy(c->vfn.d.data(), v, n * sizeof(double));
+    std::memcpy(c->wfn.d.data(), w, n * sizeof(double));
+    std::memcpy(c->pfn.d.data(), p, n * sizeof(double));
+    BCglobalVC(*c, c->ufn, c->vfn, c->wfn, c->ufv, c->vfv, c->wfv, 3);
+    BCglobalP(*c, c->pfn, c->pfv, 3);
+    interpolateU(*c, c->ufn, c->vfn, c->wfn);
+    std::fill(c->rhsuf.d.begin(), c->rhsuf.d.end(), 0.0);
+    std::fill(c->rhsvf.d.begin(), c->rhsvf.d.end(), 0.0);
+    std::fill(c->rhswf.d.begin(), c->rhswf.d.end(), 0.0);
+    // LoopTimeInitial: (n+1) = (n)
+    c->ufnp = c->ufn; c->vfnp = c->vfn; c->wfnp = c->wfn; c->pfnp = c->pfn;
+    c->flag_ab = 0;
+    return 0;
+}
+
+int orc_get(const orc_ctx* cc, int field, double* out) {
+    R2* a = field_ptr(const_cast<orc_ctx&>(*cc), field);
+    if (!a) return -1;
+    std::memcpy(out, a->d.data(), a->d.size() * sizeof(double));
+    return (int)a->d.size();
+}
+
+int orc_set(orc_ctx* c, int field, const double* in) {
+    R2* a = field_ptr(*c, field);
+    if (!a) return -1;
+    std::memcpy(a->d.data(), in, a->d.size() * sizeof(double));
+    return 0;
+}
+
+int orc_get_flag_ab(const orc_ctx* c) { return c->flag_ab; }
+void orc_set_flag_ab(orc_ctx* c, int f) { c->flag_ab = f; }
+
+int orc_step(orc_ctx* c, int fin_rk, orc_info* info) {
+    set_threads(*c);
+    const int NC = c->NC, NZ = c->NZ;
+    // (known) = (n): nsmp3D.F90:419-441
+    c->uf = c->ufn; c->vf = c->vfn; c->wf = c->wfn; c->pf = c->pfn;
+    int nstage = (fin_rk == 3) ? 3 : (fin_rk == 2 ? 2 : 1);
+    int max_it = 0;
+    for (int s = 1; s <= nstage; ++s) {
+        hydro(*c, fin_rk);
+        max_it = std::max(max_it, c->info.iters);
+        if (fin_rk == 3 && s == 2) {
+            // SSP-RK3 combination of cell velocities (extension)
+            for (size_t q = 0; q < (size_t)NC * NZ; ++q) {
+                c->ufnp.d[q] = 0.75 * c->ufn.d[q] + 0.25 * c->ufnp.d[q];
+                c->vfnp.d[q] = 0.75 * c->vfn.d[q] + 0.25 * c->vfnp.d[q];
+                c->wfnp.d[q] = 0.75 * c->wfn.d[q] + 0.25 * c->wfnp.d[q];
+            }
+        }
+        if (s < nstage) {  // (known) = (n+1): nsmp3D.F90:480-504
+            c->uf = c->ufnp; c->vf = c->vfnp; c->wf = c->wfnp; c->pf = c->pfnp;
+        }
+    }
+    if (fin_rk == 2) {  // nsmp3D.F90:531-546
+        for (size_t q = 0; q < (size_t)NC * NZ; ++q) {
+            c->ufnp.d[q] = 0.5 * (c->ufn.d[q] + c->ufnp.d[q]);
+            c->vfnp.d[q] = 0.5 * (c->vfn.d[q] + c->vfnp.d[q]);
+            c->wfnp.d[q] = 0.5 * (c->wfn.d[q] + c->wfnp.d[q]);
+        }
+    } else if (fin_rk == 3) {
+        for (size_t q = 0; q < (size_t)NC * NZ; ++q) {
+            c->ufnp.d[q] = (1.0 / 3.0) * c->ufn.d[q] + (2.0 / 3.0) * c->ufnp.d[q];
+            c->vfnp.d[q] = (1.0 / 3.0) * c->vfn.d[q] + (2.0 / 3.0) * c->vfnp.d[q];
+            c->wfnp.d[q] = (1.0 / 3.0) * c->wfn.d[q] + (2.0 / 3.0) * c->wfnp.d[q];
+        }
+    }
+    // LoopTimeUpdate: (n) = (n+1)
+    c->ufn = c->ufnp; c->vfn = c->vfnp; c->wfn = c->wfnp; c->pfn = c->pfnp;
+    if (info) { *info = c->info; info->iters = max_it; }
+    return c->info.converged ? 0 : 1;
+}
+
+int orc_apply_A(orc_ctx* c, const double* x, double* y) {
+    R2 in, out;
+    in.init(c->NC, c->NZ); out.init(c->NC, c->NZ);
+    std::memcpy(in.d.data(), x, in.d.size() * sizeof(double));
+    get_Apk(*c, out, in);
+    std::memcpy(y, out.d.data(), out.d.size() * sizeof(double));
+    return 0;
+}
+
+int orc_gradient_lsm(orc_ctx* c, const double* f, double* dfdx, double* dfdy, double* dfds) {
+    R2 fun, a, b, d;
+    fun.init(c->NC, c->NZ); a.init(c->NC, c->NZ); b.init(c->NC, c->NZ); d.init(c->NC, c->NZ);
+    std::memcpy(fun.d.data(), f, fun.d.size() * sizeof(double));
+    grandientLSM(*c, a, b, d, fun);
+    std::memcpy(dfdx, a.d.data(), a.d.size() * sizeof(double));
+    std::memcpy(dfdy, b.d.data(), b.d.size() * sizeof(double));
+    std::memcpy(dfds, d.d.data(), d.d.size() * sizeof(double));
+    return 0;
+}
+
+int orc_vertex_interp(orc_ctx* c, const double* f, int is_pressure, int tagBC, int tagdir, double* fv) {
+    R2 fun, v;
+    fun.init(c->NC, c->NZ); v.init(c->NV, c->NZ - 1);
+    std::memcpy(fun.d.data(), f, fun.d.size() * sizeof(double));
+    if (is_pressure) BCglobalP(*c, fun, v, tagdir);
+    else {
+        BCvelcenter3D(*c, fun, tagBC);
+        interpolation3D(*c, v, fun, tagdir);
+        BCvelvertex3D(*c, v, tagBC, tagdir);
+    }
+    std::memcpy(fv, v.d.data(), v.d.size() * sizeof(double));
+    return 0;
+}
+
+int orc_mass_diag(orc_ctx* c, double* out) {
+    const int N0 = c->N0, NZ = c->NZ;
+    double sabs = 0, smax = 0, ssum = 0, cfl = 0;
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            double dsv = c->dsigv(k - 1);
+            double flux = 0.0, fc = 0.0;
+            flux = flux + c->U1FACE(i, k) * c->dlVV(i, 1) * dsv;
+            flux = flux + c->U2FACE(i, k) * c->dlVV(i, 2) * dsv;
+            flux = flux + c->U3FACE(i, k) * c->dlVV(i, 3) * dsv;
+            flux = flux + c->UTFACE(i, k) * c->areaCell(i);
+            flux = flux + c->UBFACE(i, k) * c->areaCell(i);
+            fc += std::fabs(c->U1FACE(i, k) * c->dlVV(i, 1) * dsv) + std::fabs(c->U2FACE(i, k) * c->dlVV(i, 2) * dsv) +
+                  std::fabs(c->U3FACE(i, k) * c->dlVV(i, 3) * dsv) + std::fabs(c->UBFACE(i, k) * c->areaCell(i)) +
+                  std::fabs(c->UTFACE(i, k) * c->areaCell(i));
+            fc = 0.5 * c->P.dt * fc / (c->areaCell(i) * dsv);
+            cfl = std::max(cfl, fc);
+            sabs += std::fabs(flux);
+            smax = std::max(smax, std::fabs(flux));
+            ssum += flux;
+        }
+    out[0] = sabs; out[1] = smax; out[2] = ssum; out[3] = cfl;
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,180 @@
+"""ctypes binding of the CPU oracle -- test infrastructure only.
+
+Imported by tests/, by __graft_entry__.smoke() (as the checker) and by the
+CPU-baseline leg of bench.py.  Arrays are numpy arrays in the reference's
+Fortran layout (column-major, 1-based index values).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+F_U, F_V, F_W, F_P, F_U1F, F_U2F, F_U3F, F_UTF, F_UBF, F_RHSU, F_RHSV, F_RHSW, \
+    F_EDDY, F_UV, F_VV, F_WV, F_PV = range(17)
+
+(G_XC, G_YC, G_AREA, G_DLVV, G_DLCC, G_DLE1, G_DLE2, G_DOE, G_XNN, G_YNN,
+ G_DXCC, G_DYCC, G_SUMXC2, G_SUMYC2, G_SUMXCYC, G_SIG, G_DSIG, G_SIGV, G_DSIGV,
+ G_AMC0, G_AMC1, G_AMC2, G_AMC3, G_AMCT, G_AMCB, G_DLVSUM) = range(26)
+
+
+class OrcParams(C.Structure):
+    _fields_ = [
+        ("n0", C.c_int), ("nvert", C.c_int), ("nz", C.c_int),
+        ("xdini", C.c_double), ("xdfin", C.c_double),
+        ("ydini", C.c_double), ("ydfin", C.c_double),
+        ("sigini", C.c_double), ("sigfin", C.c_double),
+        ("grid_kind", C.c_int), ("grid_beta", C.c_double),
+        ("top_bc", C.c_int), ("bot_bc", C.c_int),
+        ("dt", C.c_double), ("re", C.c_double),
+        ("bdx", C.c_double), ("bdy", C.c_double), ("bdz", C.c_double),
+        ("eps", C.c_double), ("max_iters", C.c_int),
+        ("les", C.c_int), ("les_van", C.c_int),
+        ("ref_bug_compat", C.c_int), ("nthreads", C.c_int),
+    ]
+
+
+class OrcInfo(C.Structure):
+    _fields_ = [("iters", C.c_int), ("e1norm", C.c_double), ("e2norm", C.c_double),
+                ("converged", C.c_int), ("max_eddy", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        L = C.CDLL(path)
+        P = C.POINTER
+        L.orc_create.restype = C.c_void_p
+        L.orc_create.argtypes = [P(OrcParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_void_p, P(C.c_int)]
+        L.orc_destroy.argtypes = [C.c_void_p]
+        for name in ("orc_ncell", "orc_get_flag_ab"):
+            getattr(L, name).argtypes = [C.c_void_p]
+            getattr(L, name).restype = C.c_int
+        L.orc_set_flag_ab.argtypes = [C.c_void_p, C.c_int]
+        L.orc_ghost_image.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_no_cp.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_geom.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.orc_user_initial.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+        L.orc_get.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.orc_set.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.orc_step.argtypes = [C.c_void_p, C.c_int, P(OrcInfo)]
+        L.orc_apply_A.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_gradient_lsm.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+        L.orc_vertex_interp.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        L.orc_mass_diag.argtypes = [C.c_void_p, C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """One oracle context: geometry from a mesh, then reference time steps."""
+
+    def __init__(self, params: dict, mesh: dict, nthreads: int = 0):
+        L = lib()
+        p = OrcParams()
+        for name, _ in OrcParams._fields_:
+            if name == "nthreads":
+                continue
+            setattr(p, name, params[name])
+        p.nthreads = nthreads
+        self.params = dict(params)
+        self.mesh = {k: np.asfortranarray(v, dtype=(np.int32 if k in ("No_vp", "No_cp", "nbe", "nbev") else np.float64))
+                     for k, v in mesh.items()}
+        err = C.c_int(0)
+        m = self.mesh
+        self.h = L.orc_create(C.byref(p), _ptr(m["No_vp"]), _ptr(m["No_cp"]), _ptr(m["nbe"]),
+                              _ptr(m["nbev"]), _ptr(m["xv"]), _ptr(m["yv"]), C.byref(err))
+        if not self.h:
+            raise RuntimeError(f"orc_create failed with {err.value}")
+        self.n0, self.nvert, self.nz = params["n0"], params["nvert"], params["nz"]
+        self.ncell = L.orc_ncell(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def shape(self, field):
+        if field in (F_U1F, F_U2F, F_U3F, F_UTF, F_UBF):
+            return (self.n0, self.nz)
+        if field in (F_UV, F_VV, F_WV, F_PV):
+            return (self.nvert, self.nz - 1)
+        return (self.ncell, self.nz)
+
+    def get(self, field):
+        out = np.zeros(self.shape(field), dtype=np.float64, order="F")
+        lib().orc_get(self.h, field, _ptr(out))
+        return out
+
+    def set(self, field, arr):
+        a = np.asfortranarray(arr, dtype=np.float64)
+        assert a.shape == self.shape(field)
+        lib().orc_set(self.h, field, _ptr(a))
+
+    def geom(self, which, shape):
+        out = np.zeros(shape, dtype=np.float64, order="F")
+        lib().orc_geom(self.h, which, _ptr(out))
+        return out
+
+    def ghost_image(self):
+        img = np.zeros(self.ncell - self.n0, dtype=np.int32)
+        lib().orc_ghost_image(self.h, _ptr(img))
+        return img
+
+    def no_cp(self):
+        out = np.zeros((self.ncell, 3), dtype=np.int32, order="F")
+        lib().orc_no_cp(self.h, _ptr(out))
+        return out
+
+    def user_initial(self, u, v, w, p):
+        arrs = [np.asfortranarray(a, dtype=np.float64) for a in (u, v, w, p)]
+        for a in arrs:
+            assert a.shape == (self.ncell, self.nz)
+        lib().orc_user_initial(self.h, *[_ptr(a) for a in arrs])
+
+    def step(self, fin_rk=1):
+        info = OrcInfo()
+        rc = lib().orc_step(self.h, fin_rk, C.byref(info))
+        return rc, {"iters": info.iters, "e1norm": info.e1norm, "e2norm": info.e2norm,
+                    "converged": info.converged, "max_eddy": info.max_eddy}
+
+    @property
+    def flag_ab(self):
+        return lib().orc_get_flag_ab(self.h)
+
+    @flag_ab.setter
+    def flag_ab(self, f):
+        lib().orc_set_flag_ab(self.h, int(f))
+
+    def apply_A(self, x):
+        x = np.asfortranarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        lib().orc_apply_A(self.h, _ptr(x), _ptr(y))
+        return y
+
+    def gradient_lsm(self, f):
+        f = np.asfortranarray(f, dtype=np.float64)
+        outs = [np.zeros_like(f) for _ in range(3)]
+        lib().orc_gradient_lsm(self.h, _ptr(f), *[_ptr(o) for o in outs])
+        return outs
+
+    def vertex_interp(self, f, is_pressure=True, tag_bc=0, tagdir=2):
+        f = np.asfortranarray(f, dtype=np.float64)
+        out = np.zeros((self.nvert, self.nz - 1), dtype=np.float64, order="F")
+        lib().orc_vertex_interp(self.h, _ptr(f), int(is_pressure), int(tag_bc), int(tagdir), _ptr(out))
+        return out
+
+    def mass_diag(self):
+        out = np.zeros(4, dtype=np.float64)
+        lib().orc_mass_diag(self.h, _ptr(out))
+        return out

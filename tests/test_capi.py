@@ -1,0 +1,73 @@
+"""The C-ABI library loads without a GPU and exports every entry point the
+public header declares; host-only entry points work on the CPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import nsmp_gb300 as ng
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    names = []
+    for h in sorted(os.listdir(os.path.join(REPO, "include"))):
+        if not h.endswith(".h"):
+            continue
+        src = open(os.path.join(REPO, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_\s\*]*?\b(nsmp_[a-z0-9_]+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_header():
+    L = ng.lib()
+    names = header_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    assert set(ng.EXPORTS) <= set(names)
+
+
+def test_mesh_generator_shapes_and_determinism():
+    m1 = ng.make_mesh(8, 6, seed=0)
+    m2 = ng.make_mesh(8, 6, seed=0)
+    m3 = ng.make_mesh(8, 6, seed=7)
+    for k in m1:
+        assert np.array_equal(m1[k], m2[k])
+    assert not np.array_equal(m1["xv"], m3["xv"])
+    assert m1["No_vp"].shape == (96, 3) and m1["xv"].shape == (63,)
+    # neighbour symmetry: j is a neighbour of i iff i is a neighbour of j
+    cp = m1["No_cp"]
+    for i in range(cp.shape[0]):
+        for j in range(3):
+            n = cp[i, j]
+            if n:
+                assert (i + 1) in cp[n - 1]
+    assert np.count_nonzero(cp == 0) == 2 * (8 + 6)
+
+
+def test_initial_channel_keyed_by_cell():
+    prm = ng.channel_params(8, 6, 6, 1e-3)
+    ncell = ng.n_cell_of(ng.make_mesh(8, 6))
+    u, v, w, p = ng.initial_channel(prm, ncell, seed=1)
+    u2, _, _, _ = ng.initial_channel(prm, ncell + 10, seed=1)
+    # the value of a cell does not depend on the array it is written into
+    assert np.array_equal(u[:prm["n0"]], u2[:prm["n0"]])
+    assert np.all(u[prm["n0"]:] == 0) and np.all(p == 0)
+    sig = ng.geometry(prm, ng.make_mesh(8, 6), ng.G_SIG)
+    k = 3
+    prof = 18.0 * sig[k] * (2 - sig[k])
+    assert np.all(np.abs(u[:prm["n0"], k] - prof) <= 1.8)
+    assert np.all(u[:prm["n0"], 0] == 0)  # ghost layer below the wall
+
+
+def test_bad_mesh_arguments():
+    L = ng.lib()
+    n0, nv = C.c_int(), C.c_int()
+    assert L.nsmp_mesh_size(1, 5, C.byref(n0), C.byref(nv)) == ng.ERR_ARG
+    with pytest.raises(ValueError):
+        ng.make_mesh(8, 6, jitter=0.9)
