@@ -30,10 +30,11 @@ int nsmp_create(const nsmp_params* prm, const nsmp_mesh* mesh, nsmp_ctx** out) {
     try {
         c->prm = *prm;
         c->device = prm->device;
-        if (prm->precision != NSMP_FP64) {
+        if (prm->precision != NSMP_FP64 && prm->precision != NSMP_MIXED) {
             delete c;
-            return NSMP_ERR_UNSUPPORTED;
+            return NSMP_ERR_ARG;
         }
+        c->precision = prm->precision;
         std::string err;
         int rc = nsmp::build_layout(*prm, *mesh, c->L, err);
         if (rc != 0) {
@@ -185,8 +186,9 @@ int nsmp_time_update(nsmp_ctx* c) {
 // composition u1 = S(u^n), u2 = 3/4 u^n + 1/4 S(u1), u^n+1 = 1/3 u^n + 2/3 S(u2)
 // of the same stage (pressure and face fluxes taken from the last stage,
 // as the reference's RK2 does).
-int nsmp_step(nsmp_ctx* c, int fin_rk, int nsteps, nsmp_stage_info* last) {
+int nsmp_step(nsmp_ctx* c, int fin_rk, int nsteps, int* flag_ab, nsmp_stage_info* last) {
     if (!c || fin_rk < 1 || fin_rk > 3 || nsteps < 0) return NSMP_ERR_ARG;
+    if (flag_ab) c->flag_ab = *flag_ab;
     int worst = 0;
     for (int s = 0; s < nsteps; ++s) {
         nsmp_copy_known_from_n(c);
@@ -213,6 +215,7 @@ int nsmp_step(nsmp_ctx* c, int fin_rk, int nsteps, nsmp_stage_info* last) {
         nsmp_time_update(c);
         if (last) *last = inf;
     }
+    if (flag_ab) *flag_ab = c->flag_ab;
     return worst;
 }
 
@@ -222,9 +225,13 @@ int nsmp_mass_diag(nsmp_ctx* c, double out[4]) {
 }
 
 int nsmp_set_precision(nsmp_ctx* c, int mode) {
-    if (!c) return NSMP_ERR_ARG;
-    if (mode != NSMP_FP64) return set_err(c, NSMP_ERR_UNSUPPORTED, "only NSMP_FP64 is built");
+    if (!c || (mode != NSMP_FP64 && mode != NSMP_MIXED)) return NSMP_ERR_ARG;
+    if (mode == NSMP_MIXED && !c->b64) {
+        int rc = nsmp::mixed_alloc(c);
+        if (rc) return rc;
+    }
     c->precision = mode;
+    c->prm.precision = mode;
     return NSMP_OK;
 }
 

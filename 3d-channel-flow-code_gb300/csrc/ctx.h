@@ -37,6 +37,15 @@ struct nsmp_ctx {
     // Krylov work vectors
     double *x = nullptr, *r = nullptr, *r0 = nullptr, *pk = nullptr, *vk = nullptr, *sk = nullptr,
            *tk = nullptr, *invD = nullptr;
+    double* ahat[5] = {};         // Jacobi-scaled PPE couplings (A D^-1 off-diagonals)
+    // mixed precision (NSMP_MIXED): FP64 refinement vectors + FP32 inner Krylov vectors
+    double *b64 = nullptr, *xa = nullptr, *xb = nullptr;
+    float *r32 = nullptr, *r032 = nullptr, *p32[2] = {}, *v32[2] = {}, *s32 = nullptr, *t32 = nullptr,
+          *e32 = nullptr, *invD32 = nullptr, *lev32 = nullptr;
+    nsmp::ColPPE32* d_ppe32 = nullptr;
+    double inner_tol = 1e-4;
+    int last_outer = 0;
+    int last_inner_chunk = 16;
     double* stage_buf = nullptr;  // (N_CELL,NZ) staging for transfers
     // reductions and scalars
     nsmp::RedScratch red{}, red2{};
@@ -71,6 +80,10 @@ int run_scatter(nsmp_ctx* c, const double* host, double* dfield);
 int run_mass_diag(nsmp_ctx* c, double out[4]);
 int run_download_pv(nsmp_ctx* c, double* host);
 int cuda_fail(nsmp_ctx* c, cudaError_t e, const char* where);
+int mixed_alloc(nsmp_ctx* c);
+// Pressure solve of one stage in mixed precision; on return *x_final points
+// at the FP64 solution (before the Glob_Norm mean removal).
+int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final);
 int prof_begin(nsmp_ctx* c, int kid);   // returns event slot or -1
 void prof_end(nsmp_ctx* c, int slot);
 int prof_resolve(nsmp_ctx* c);

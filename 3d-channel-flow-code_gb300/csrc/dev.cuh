@@ -26,6 +26,10 @@ struct Scal {
     int iter, done, converged, status;
     int max_iters, pad;
     double eps;
+    // mixed precision: inner FP32 BiCGSTAB state and outer refinement count
+    double ib1, ib2, ir1, ir2, irho, irho_prev, ialpha, iomega, ir0v;
+    double inner_tol;
+    int iiter, idone, outer, pad2;
 };
 
 // Everything a kernel needs to address the mesh; passed by value.

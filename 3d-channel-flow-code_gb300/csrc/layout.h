@@ -32,6 +32,14 @@ struct ColPPE {
     double area;
 };
 
+// FP32 copy of ColPPE for the mixed-precision inner solver.
+struct ColPPE32 {
+    int nb[3];
+    float kA[3];
+    float area;
+    float pad;
+};
+
 // Coefficients of one column used by the stage kernels.
 struct ColGeo {
     int nb[3];       // neighbour column across edge j

@@ -307,7 +307,7 @@ int build_layout(const nsmp_params& p, const nsmp_mesh& m, HostLayout& L, std::s
         err = "TopBC/BotBC must be 0 (no-slip) or 1 (free-slip)";
         return NSMP_ERR_UNSUPPORTED;
     }
-    if (!(p.dt > 0.0) || !(p.re > 0.0) || !(p.eps > 0.0) || p.max_iters < 1) { err = "bad dt/Re/eps/MaxIters"; return NSMP_ERR_ARG; }
+    if (!(p.dt > 0.0) || !(p.re > 0.0) || !(p.eps > 0.0) || p.max_iters < 0) { err = "bad dt/Re/eps/MaxIters"; return NSMP_ERR_ARG; }
     Geo g;
     g.N0 = p.n0; g.NV = p.nvert; g.NZ = p.nz;
     g.vp.resize(3 * (size_t)g.N0); g.cp.resize(3 * (size_t)g.N0);

@@ -17,15 +17,10 @@
 #include <cmath>
 #include <cstdio>
 
-#include "ctx.h"
+#include "kern_common.cuh"
 
 namespace nsmp {
 namespace {
-
-__device__ __forceinline__ void prism_of(const Mesh& m, int g, int& c, int& k0) {
-    c = g / m.NZI;
-    k0 = 1 + (g - c * m.NZI);
-}
 
 // ---------------------------------------------------------------------------
 // Vertex interpolation: interpolation2D (interpolation2D.F90:120-135) with
@@ -246,18 +241,6 @@ __global__ void __launch_bounds__(kBlock) k_faces_div(Mesh m, FaceArgs a, RedScr
     }
 }
 
-// PPE row (PDE.F90:69-121) applied to a field: returns sum of the six
-// coefficient products in the reference's order.
-__device__ __forceinline__ double ppe_row(const Mesh& m, const ColPPE& P, int k0, double x0, double x1, double x2,
-                                          double x3, double xT, double xB) {
-    const double dsv = lev(m, LV_DSV, k0);
-    const double AA1 = P.kA[0] * dsv, AA2 = P.kA[1] * dsv, AA3 = P.kA[2] * dsv;
-    const double AAB = P.area * lev(m, LV_IDSB, k0) * lev(m, LV_WB, k0);
-    const double AAT = P.area * lev(m, LV_IDST, k0) * lev(m, LV_WT, k0);
-    const double AA0 = -1.0 * (AAT + AAB + AA1 + AA2 + AA3);
-    return AA0 * x0 + AA1 * x1 + AA2 * x2 + AA3 * x3 + AAT * xT + AAB * xB;
-}
-
 // Jacobi diagonal 1/Am0 (diag_precdt, bicgstab.F90:831-836), once at setup.
 __global__ void k_inv_diag(Mesh m, double* invD) {
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
@@ -277,6 +260,7 @@ struct KryArgs {
     const double* pf;
     double *x, *r, *r0, *p, *v, *s, *t;
     const double* invD;
+    const double* ah[5];   // Jacobi-scaled couplings: nb 1..3, top, bottom
 };
 
 // Glob_Norm(rhs, 1) + initial residual and norms (bicgstab.F90:107-109,
@@ -330,9 +314,10 @@ __global__ void __launch_bounds__(kBlock) k_bicg_p(Mesh m, KryArgs a, const Scal
     }
 }
 
-// y = D^-1 in (diag_precdt), out = A y (get_Apk, bicgstab.F90:976-997) and
-// the fused dot products.  MODE 0: v = A D^-1 p, dot (r0, v);
-// MODE 1: t = A D^-1 s, dots (t, s), (t, t).
+// out = A D^-1 in (diag_precdt then get_Apk, bicgstab.F90:831-836, 976-997)
+// with the Jacobi-scaled coefficients ahat_j = A_ij / A_jj precomputed once
+// (the diagonal of A D^-1 is 1), and the fused dot products.
+// MODE 0: v = A D^-1 p, dot (r0, v);  MODE 1: t = A D^-1 s, dots (t, s), (t, t).
 template <int MODE>
 __global__ void __launch_bounds__(kBlock) k_bicg_spmv(Mesh m, KryArgs a, RedScratch rs, Scal* sc) {
     if (sc->done) return;
@@ -344,20 +329,20 @@ __global__ void __launch_bounds__(kBlock) k_bicg_spmv(Mesh m, KryArgs a, RedScra
         prism_of(m, g, c, k0);
         const ColPPE& P = m.ppe[c];
         const size_t q = IX(m, c, k0);
-        const size_t q1 = IX(m, P.nb[0], k0), q2 = IX(m, P.nb[1], k0), q3 = IX(m, P.nb[2], k0);
-        const double y0 = in[q] * a.invD[q];
-        const double y1 = in[q1] * a.invD[q1], y2 = in[q2] * a.invD[q2], y3 = in[q3] * a.invD[q3];
+        const double x0 = in[q];
+        double o = x0;
+        o = fma(a.ah[0][q], in[IX(m, P.nb[0], k0)], o);
+        o = fma(a.ah[1][q], in[IX(m, P.nb[1], k0)], o);
+        o = fma(a.ah[2][q], in[IX(m, P.nb[2], k0)], o);
         // wall layers carry zero coefficients (AmB(i,2) = AmT(i,NZ-1) = 0)
-        const double yT = (k0 < m.NZ - 2) ? in[q + 1] * a.invD[q + 1] : 0.0;
-        const double yB = (k0 > 1) ? in[q - 1] * a.invD[q - 1] : 0.0;
-        const double o = ppe_row(m, P, k0, y0, y1, y2, y3, yT, yB);
+        o = fma(a.ah[3][q], in[q + 1], o);
+        o = fma(a.ah[4][q], in[q - 1], o);
         out[q] = o;
         if (MODE == 0) {
-            part[0] += a.r0[q] * o;
+            part[0] = fma(a.r0[q], o, part[0]);
         } else {
-            const double sv = in[q];
-            part[0] += o * sv;
-            part[1] += o * o;
+            part[0] = fma(o, x0, part[0]);
+            part[1] = fma(o, o, part[1]);
         }
     }
     double tot[2];
@@ -374,6 +359,24 @@ __global__ void __launch_bounds__(kBlock) k_bicg_spmv(Mesh m, KryArgs a, RedScra
             sc->tt = tot[1];
             sc->omega = tot[0] / tot[1];
         }
+    }
+}
+
+// Scaled coefficients ahat = A_ij * (1/A_jj) of the five off-diagonal
+// couplings, once at setup; zero at the walls.
+__global__ void k_scaled_coefs(Mesh m, const double* __restrict__ invD, double* a1, double* a2, double* a3,
+                               double* aT, double* aB) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const ColPPE& P = m.ppe[c];
+        const size_t q = IX(m, c, k0);
+        const double dsv = lev(m, LV_DSV, k0);
+        a1[q] = (P.kA[0] * dsv) * invD[IX(m, P.nb[0], k0)];
+        a2[q] = (P.kA[1] * dsv) * invD[IX(m, P.nb[1], k0)];
+        a3[q] = (P.kA[2] * dsv) * invD[IX(m, P.nb[2], k0)];
+        aT[q] = (k0 < m.NZ - 2) ? (P.area * lev(m, LV_IDST, k0)) * invD[q + 1] : 0.0;
+        aB[q] = (k0 > 1) ? (P.area * lev(m, LV_IDSB, k0)) * invD[q - 1] : 0.0;
     }
 }
 
@@ -400,7 +403,7 @@ __global__ void __launch_bounds__(kBlock) k_bicg_x(Mesh m, KryArgs a, RedScratch
         prism_of(m, g, c, k0);
         const size_t q = IX(m, c, k0);
         const double id = a.invD[q];
-        const double xn = a.x[q] + al * (a.p[q] * id) + om * (a.s[q] * id);
+        const double xn = fma(id, fma(om, a.s[q], al * a.p[q]), a.x[q]);
         const double res = a.s[q] - om * a.t[q];
         a.x[q] = xn;
         a.r[q] = res;
@@ -588,31 +591,12 @@ __global__ void __launch_bounds__(kBlock) k_mass_diag(Mesh m, const double* f1, 
     if (grid_reduce<2, true>(mx, rs2, tm) && threadIdx.x == 0) { sc->diag[1] = tm[0]; sc->diag[3] = tm[1]; }
 }
 
-int grid_for(const nsmp_ctx* c, long long n) {
-    long long b = (n + kBlock - 1) / kBlock;
-    long long cap = (long long)c->num_sms * 8;
-    if (b > cap) b = cap;
-    if (b < 1) b = 1;
-    return (int)b;
-}
-
 }  // namespace
 
 int cuda_fail(nsmp_ctx* c, cudaError_t e, const char* where) {
     c->err = std::string(where) + ": " + cudaGetErrorString(e);
     return NSMP_ERR_CUDA;
 }
-
-#define CK(call)                                                  \
-    do {                                                          \
-        cudaError_t e_ = (call);                                  \
-        if (e_ != cudaSuccess) return cuda_fail(c, e_, #call);    \
-    } while (0)
-#define CKL(where)                                                \
-    do {                                                          \
-        cudaError_t e_ = cudaGetLastError();                      \
-        if (e_ != cudaSuccess) return cuda_fail(c, e_, where);    \
-    } while (0)
 
 int prof_begin(nsmp_ctx* c, int kid) {
     if (!c->prof_on) return -1;
@@ -648,14 +632,6 @@ int prof_resolve(nsmp_ctx* c) {
     c->ev_used = 0;
     return 0;
 }
-
-#define LAUNCH(KID, ...)                         \
-    do {                                         \
-        const int slot_ = prof_begin(c, (KID));  \
-        __VA_ARGS__;                             \
-        prof_end(c, slot_);                      \
-        ++c->launches;                           \
-    } while (0)
 
 int run_user_initial(nsmp_ctx* c) {
     const Mesh& m = c->mesh;
@@ -719,38 +695,45 @@ int run_stage(nsmp_ctx* c, int fin_rk, nsmp_stage_info* info) {
                 c->face[3], c->face[4], c->rhsp, 1.0 / P.dt, 1};
     LAUNCH(NSMP_K_FACES_DIV, k_faces_div<<<gp, kBlock, 0, st>>>(m, fa, c->red, c->d_scal));
     CKL("k_faces_div");
-    KryArgs ka{c->rhsp, K[3], c->x, c->r, c->r0, c->pk, c->vk, c->sk, c->tk, c->invD};
-    LAUNCH(NSMP_K_BICG_INIT, k_bicg_init<<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
-    CKL("k_bicg_init");
-    // BiCGSTAB iterations, enqueued in chunks; every kernel returns at once
-    // after the device-side stopping test has fired.
-    int chunk = c->last_iters > 2 ? c->last_iters - 1 : 2;
-    int launched = 0;
-    for (;;) {
-        for (int it = 0; it < chunk; ++it) {
-            LAUNCH(NSMP_K_BICG_P, k_bicg_p<<<gp, kBlock, 0, st>>>(m, ka, c->d_scal));
-            LAUNCH(NSMP_K_BICG_SPMV_V, k_bicg_spmv<0><<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
-            LAUNCH(NSMP_K_BICG_S, k_bicg_s<<<gp, kBlock, 0, st>>>(m, ka, c->d_scal));
-            LAUNCH(NSMP_K_BICG_SPMV_T, k_bicg_spmv<1><<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
-            LAUNCH(NSMP_K_BICG_X, k_bicg_x<<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
+    const double* xsol = c->x;
+    if (c->precision == NSMP_MIXED) {
+        int rc = run_pressure_mixed(c, K[3], &xsol);
+        if (rc) return rc;
+    } else {
+        KryArgs ka{c->rhsp, K[3], c->x, c->r, c->r0, c->pk, c->vk, c->sk, c->tk, c->invD,
+                   {c->ahat[0], c->ahat[1], c->ahat[2], c->ahat[3], c->ahat[4]}};
+        LAUNCH(NSMP_K_BICG_INIT, k_bicg_init<<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
+        CKL("k_bicg_init");
+        // BiCGSTAB iterations, enqueued in chunks; every kernel returns at once
+        // after the device-side stopping test has fired.
+        int chunk = c->last_iters > 2 ? c->last_iters - 1 : 2;
+        int launched = 0;
+        for (;;) {
+            for (int it = 0; it < chunk; ++it) {
+                LAUNCH(NSMP_K_BICG_P, k_bicg_p<<<gp, kBlock, 0, st>>>(m, ka, c->d_scal));
+                LAUNCH(NSMP_K_BICG_SPMV_V, k_bicg_spmv<0><<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
+                LAUNCH(NSMP_K_BICG_S, k_bicg_s<<<gp, kBlock, 0, st>>>(m, ka, c->d_scal));
+                LAUNCH(NSMP_K_BICG_SPMV_T, k_bicg_spmv<1><<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
+                LAUNCH(NSMP_K_BICG_X, k_bicg_x<<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
+            }
+            CKL("bicgstab iteration");
+            launched += chunk;
+            CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            prof_resolve(c);
+            if (c->h_scal->done) break;
+            if (launched > P.max_iters + 8) {  // cannot happen: the device test stops at MaxIters
+                c->err = "BiCGSTAB did not stop";
+                return NSMP_ERR_CUDA;
+            }
+            chunk = 4;
         }
-        CKL("bicgstab iteration");
-        launched += chunk;
-        CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        prof_resolve(c);
-        if (c->h_scal->done) break;
-        if (launched > P.max_iters + 8) {  // cannot happen: the device test stops at MaxIters
-            c->err = "BiCGSTAB did not stop";
-            return NSMP_ERR_CUDA;
-        }
-        chunk = 4;
     }
-    LAUNCH(NSMP_K_PMEAN, k_pmean<<<gp, kBlock, 0, st>>>(m, c->x, c->red, c->d_scal));
+    LAUNCH(NSMP_K_PMEAN, k_pmean<<<gp, kBlock, 0, st>>>(m, xsol, c->red, c->d_scal));
     CKL("k_pmean");
-    LAUNCH(NSMP_K_VERTEX1, k_vertex1<<<gv, kBlock, 0, st>>>(m, c->x, c->d_scal, c->vtx[3]));
+    LAUNCH(NSMP_K_VERTEX1, k_vertex1<<<gv, kBlock, 0, st>>>(m, xsol, c->d_scal, c->vtx[3]));
     CKL("k_vertex1");
-    ProjArgs pa{c->x, c->vtx[3], c->ustar[0], c->ustar[1], c->ustar[2], c->face[0], c->face[1], c->face[2],
+    ProjArgs pa{xsol, c->vtx[3], c->ustar[0], c->ustar[1], c->ustar[2], c->face[0], c->face[1], c->face[2],
                 c->face[3], c->face[4], N[0], N[1], N[2], N[3], P.dt};
     LAUNCH(NSMP_K_PROJECT, k_project<<<gp, kBlock, 0, st>>>(m, pa, c->d_scal));
     CKL("k_project");
@@ -844,7 +827,8 @@ int ctx_init_device(nsmp_ctx* c) {
         for (int f = 0; f < 4; ++f) CK(dalloc((void**)&c->lvl[b][f], ncf * sizeof(double)));
     for (auto** p : {&c->face[0], &c->face[1], &c->face[2], &c->face[3], &c->face[4], &c->hist[0], &c->hist[1],
                      &c->hist[2], &c->eddy, &c->ustar[0], &c->ustar[1], &c->ustar[2], &c->rhsp, &c->x, &c->r,
-                     &c->r0, &c->pk, &c->vk, &c->sk, &c->tk, &c->invD})
+                     &c->r0, &c->pk, &c->vk, &c->sk, &c->tk, &c->invD, &c->ahat[0], &c->ahat[1], &c->ahat[2],
+                     &c->ahat[3], &c->ahat[4]})
         CK(dalloc((void**)p, ncf * sizeof(double)));
     for (int f = 0; f < 4; ++f) CK(dalloc((void**)&c->vtx[f], nvf * sizeof(double)));
     const size_t stage_n = std::max((size_t)L.NC * L.NZ, (size_t)L.NV * L.NZ);
@@ -897,11 +881,16 @@ int ctx_init_device(nsmp_ctx* c) {
     m.tv_lsig = L.total_volume * L.lsig;
     k_inv_diag<<<grid_for(c, m.nprism), kBlock, 0, c->stream>>>(m, c->invD);
     CKL("k_inv_diag");
+    k_scaled_coefs<<<grid_for(c, m.nprism), kBlock, 0, c->stream>>>(m, c->invD, c->ahat[0], c->ahat[1], c->ahat[2],
+                                                                   c->ahat[3], c->ahat[4]);
+    CKL("k_scaled_coefs");
     Scal s0{};
     s0.eps = c->prm.eps;
     s0.max_iters = c->prm.max_iters;
+    s0.inner_tol = c->inner_tol;
     CK(cudaMemcpyAsync(c->d_scal, &s0, sizeof(Scal), cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    if (c->precision == NSMP_MIXED) return mixed_alloc(c);
     return 0;
 }
 

@@ -99,7 +99,7 @@ def lib(build_if_missing=True):
         getattr(L, n).argtypes = [vp]
     L.nsmp_hydro_stage.argtypes = [vp, P(C.c_int), C.c_int, P(StageInfo)]
     L.nsmp_rk_combine.argtypes = [vp, C.c_double, C.c_double]
-    L.nsmp_step.argtypes = [vp, C.c_int, C.c_int, P(StageInfo)]
+    L.nsmp_step.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(StageInfo)]
     L.nsmp_mass_diag.argtypes = [vp, vp]
     L.nsmp_set_precision.argtypes = [vp, C.c_int]
     L.nsmp_stream.argtypes = [vp]
@@ -277,7 +277,9 @@ class Solver:
 
     def step(self, fin_rk=1, nsteps=1):
         info = StageInfo()
-        rc = self._check(self.L.nsmp_step(self.h, fin_rk, nsteps, C.byref(info)))
+        fab = C.c_int(self.flag_ab)
+        rc = self._check(self.L.nsmp_step(self.h, fin_rk, nsteps, C.byref(fab), C.byref(info)))
+        self.flag_ab = fab.value
         return rc, info.as_dict()
 
     def mass_diag(self):

@@ -200,27 +200,13 @@ def run_reference(args):
     return 0
 
 
-def run_ours(args):
-    import torch
+WORDS_MIXED = {  # FP32 words (4 B) per prism of the inner kernels; FP64 words for the rest
+    "k_bicg_spmv_v": 7 * 0.5, "k_bicg_spmv_t": 5 * 0.5, "k_bicg_x": 8 * 0.5,
+}
 
-    import nsmp_gb300 as ng
 
-    world, rank, local, pg = dist_setup()
-    torch.cuda.set_device(local)
-    nx, ny, layers, dt = WORKLOADS[args.workload]
-    prisms = 2 * nx * ny * layers
-    mesh = ng.make_mesh(nx, ny)
-    prm = ng.channel_params(nx, ny, layers, dt, device=local)
-    s = ng.Solver(prm, mesh)
-    u0, v0, w0, p0 = ng.initial_channel(prm, s.ncell, seed=1)
-    s.user_initial(u0, v0, w0, p0)
-    stream = torch.cuda.ExternalStream(s.stream)
-    for _ in range(args.warmup):
-        rc, _ = s.step(3, 1)
-        if rc < 0:
-            raise RuntimeError(f"warm-up step failed: {rc}")
-
-    # ---- device-timed region: K steps, inputs resident in HBM -------------
+def timed_region(s, ng, torch, stream, steps, pg, local):
+    """K RK3 steps between CUDA events on the library's stream."""
     s.prof_enable(True)
     l0, it0 = s.counters()
     clocks = ClockSampler(local)
@@ -232,8 +218,8 @@ def run_ours(args):
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     worst = 0
-    for _ in range(args.steps):
-        rc, info = s.step(3, 1)
+    for _ in range(steps):
+        rc, _ = s.step(3, 1)
         worst = max(worst, rc)
     ev1.record(stream)
     torch.cuda.synchronize()
@@ -244,28 +230,90 @@ def run_ours(args):
     l1, it1 = s.counters()
     prof = s.prof_read()
     s.prof_enable(False)
-    ms_max = max_over_ranks(pg, ms)
-    value = world * prisms * args.steps / (ms_max / 1e3) / 1e6
-    iters_per_stage = (it1 - it0) / (3.0 * args.steps)
+    return {"ms": ms, "clocks": clk, "launches": l1 - l0, "iters": it1 - it0, "prof": prof, "status": worst}
 
-    # roofline of the dominant kernel (largest share of device time)
+
+def roofline(prof, iters, prisms, mixed):
     hbm_peak, peak_kind = load_peaks()
-    dom = max((k for k in prof if k in WORDS), key=lambda k: prof[k][1])
+    words = dict(WORDS)
+    if mixed:
+        words.update(WORDS_MIXED)
+    dom = max((k for k in prof if k in words), key=lambda k: prof[k][1])
     n_launch, dom_ms = prof[dom]
-    real_launches = n_launch
-    if dom.startswith("k_bicg_") and dom != "k_bicg_init":
-        real_launches = it1 - it0  # launches after convergence return at once
-    bytes_per_launch = WORDS[dom] * 8.0 * prisms
-    achieved = bytes_per_launch * real_launches / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    real = iters if (dom.startswith("k_bicg_") and dom != "k_bicg_init") else n_launch
+    bpl = words[dom] * 8.0 * prisms
+    achieved = bpl * real / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
     traffic = None
     tpath = os.path.join(REPO, "profiles", "ncu_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as fh:
-            tr = json.load(fh)
-        if dom in tr.get("bytes_per_prism", {}):
-            traffic = tr["bytes_per_prism"][dom] * prisms
-    fl = FLOPS.get(dom)
-    shares = {k: round(v[1] / max(sum(x[1] for x in prof.values()), 1e-12), 4) for k, v in prof.items() if v[0]}
+            tr = json.load(fh).get("mixed" if mixed else "fp64", {})
+        if dom in tr:
+            traffic = tr[dom] * prisms
+    fl = None if mixed else FLOPS.get(dom)
+    total = sum(v[1] for v in prof.values())
+    shares = {k: round(v[1] / max(total, 1e-12), 4) for k, v in prof.items() if v[0]}
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+            "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind, "traffic": traffic,
+            "algorithmic_bytes_per_launch": bpl, "avg_launch_ms": dom_ms / max(real, 1),
+            "fp64_tflops": (round(fl * prisms * real / (dom_ms / 1e3) / 1e12, 3) if fl and dom_ms > 0 else None)}
+    return roof, shares, total
+
+
+def run_ours(args):
+    import torch
+
+    import nsmp_gb300 as ng
+
+    world, rank, local, pg = dist_setup()
+    torch.cuda.set_device(local)
+    nx, ny, layers, dt = WORKLOADS[args.workload]
+    prisms = 2 * nx * ny * layers
+    mesh = ng.make_mesh(nx, ny)
+    precs = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
+    res, solvers = {}, {}
+    for prec in precs:
+        prm = ng.channel_params(nx, ny, layers, dt, device=local,
+                                precision=(ng.MIXED if prec == "mixed" else ng.FP64))
+        s = ng.Solver(prm, mesh)
+        u0, v0, w0, p0 = ng.initial_channel(prm, s.ncell, seed=1)
+        s.user_initial(u0, v0, w0, p0)
+        stream = torch.cuda.ExternalStream(s.stream)
+        for _ in range(args.warmup):
+            rc, _ = s.step(3, 1)
+            if rc < 0:
+                raise RuntimeError(f"warm-up step failed: {rc}")
+        r = timed_region(s, ng, torch, stream, args.steps, pg, local)
+        r["ms_max"] = max_over_ranks(pg, r["ms"])
+        r["value"] = world * prisms * args.steps / (r["ms_max"] / 1e3) / 1e6
+        r["roof"], r["shares"], r["busy_ms"] = roofline(r["prof"], r["iters"], prisms, prec == "mixed")
+        res[prec] = r
+        solvers[prec] = (s, stream, prm)
+    head = "mixed" if "mixed" in res else precs[0]
+    s, stream, prm = solvers[head]
+    r = res[head]
+
+    if args.profile_run:
+        if rank == 0:
+            print(json.dumps({"metric": "Mcell-steps/s", "value": r["value"], "profile_run": True,
+                              "precision": head, "kernel_share": r["shares"],
+                              "bicgstab_iters_per_stage": r["iters"] / (3.0 * args.steps)}), flush=True)
+        for sv in solvers.values():
+            sv[0].close()
+        return 0
+
+    # mixed vs FP64 after the same W + K steps from the same initial state
+    cmp = None
+    if len(res) == 2:
+        a, b = solvers["mixed"][0], solvers["fp64"][0]
+        n0 = prm["n0"]
+        cmp = {f"rel_l2_{nm}": float(np.linalg.norm(a.download(f)[:n0, 1:-1] - b.download(f)[:n0, 1:-1]) /
+                                     np.linalg.norm(b.download(f)[:n0, 1:-1]))
+               for nm, f in (("u", ng.F_U), ("v", ng.F_V), ("w", ng.F_W), ("p", ng.F_P))}
+        da, db = a.mass_diag(), b.mass_diag()
+        cmp["max_div_mixed"], cmp["max_div_fp64"] = float(da[1]), float(db[1])
+        cmp["speedup"] = res["mixed"]["value"] / res["fp64"]["value"]
+        cmp["after_steps"] = args.warmup + args.steps
 
     # ---- end to end through the C-ABI with host buffers -------------------
     pin = lambda shape: torch.empty(shape[::-1], dtype=torch.float64, pin_memory=True).numpy().T
@@ -273,12 +321,12 @@ def run_ours(args):
     h_cells = [pin((nc, nz)) for _ in range(4)]
     h_faces = [pin((prm["n0"], nz)) for _ in range(5)]
     h_hist = [pin((nc, nz)) for _ in range(3)]
-    for a, f in zip(h_cells, (ng.F_U, ng.F_V, ng.F_W, ng.F_P)):
-        a[...] = s.download(f)
-    for a, f in zip(h_faces, (ng.F_U1FACE, ng.F_U2FACE, ng.F_U3FACE, ng.F_UTFACE, ng.F_UBFACE)):
-        a[...] = s.download(f)
-    for a, f in zip(h_hist, (ng.F_RHSU, ng.F_RHSV, ng.F_RHSW)):
-        a[...] = s.download(f)
+    for hh, f in zip(h_cells, (ng.F_U, ng.F_V, ng.F_W, ng.F_P)):
+        hh[...] = s.download(f)
+    for hh, f in zip(h_faces, (ng.F_U1FACE, ng.F_U2FACE, ng.F_U3FACE, ng.F_UTFACE, ng.F_UBFACE)):
+        hh[...] = s.download(f)
+    for hh, f in zip(h_hist, (ng.F_RHSU, ng.F_RHSV, ng.F_RHSW)):
+        hh[...] = s.download(f)
     h_out = [pin((nc, nz)) for _ in range(4)]
     flag = s.flag_ab
     e2e_steps = max(1, min(args.steps, 3))
@@ -288,8 +336,8 @@ def run_ours(args):
     for _ in range(e2e_steps):
         s.upload_state(*h_cells, h_faces, h_hist, flag)
         s.step(3, 1)
-        for a, f in zip(h_out, (ng.F_U, ng.F_V, ng.F_W, ng.F_P)):
-            a[...] = s.download(f)
+        for hh, f in zip(h_out, (ng.F_U, ng.F_V, ng.F_W, ng.F_P)):
+            hh[...] = s.download(f)
     torch.cuda.synchronize()
     t_e2e = max_over_ranks(pg, time.perf_counter() - t0)
     e2e_value = world * prisms * e2e_steps / t_e2e / 1e6
@@ -308,30 +356,37 @@ def run_ours(args):
 
     if rank == 0:
         line = {
-            "metric": "Mcell-steps/s", "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "metric": "Mcell-steps/s", "value": r["value"], "unit": "Mcell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_max"] / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if head == "mixed" else "f64",
             "data": "synthetic (seeded mesh and initial state; no dataset exists for this path)",
-            "config": {"workload": workload_desc(args.workload), "prisms": prisms, "precision": "fp64",
-                       "integrator": "SSP-RK3 of the reference stage", "parallelism": "replicas" if world > 1 else "1 GPU",
-                       "l2": "inputs larger than L2 (working set ~2 GB), no flush",
-                       "bicgstab_iters_per_stage": round(iters_per_stage, 1)},
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak,
-                         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind,
-                         "traffic": traffic, "algorithmic_bytes_per_launch": bytes_per_launch,
-                         "avg_launch_ms": dom_ms / max(real_launches, 1),
-                         "fp64_tflops": (round(fl * prisms * real_launches / (dom_ms / 1e3) / 1e12, 3)
-                                         if fl and dom_ms > 0 else None)},
-            "kernel_share": shares,
+            "config": {"workload": workload_desc(args.workload), "prisms": prisms, "precision": head,
+                       "integrator": "SSP-RK3 of the reference stage",
+                       "parallelism": "replicas" if world > 1 else "1 GPU",
+                       "l2": "inputs larger than L2 (working set > 2 GB), no flush",
+                       "bicgstab_iters_per_stage": round(r["iters"] / (3.0 * args.steps), 1)},
+            "roofline": r["roof"],
+            "kernel_share": r["shares"],
+            "device_busy_frac": round(r["busy_ms"] / max(r["ms"], 1e-9), 4),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
-            "clocks": clk,
-            "gpu_launches": l1 - l0,
-            "status": worst,
+            "clocks": r["clocks"],
+            "gpu_launches": r["launches"],
+            "status": r["status"],
         }
+        if "fp64" in res and head != "fp64":
+            f = res["fp64"]
+            line["fp64"] = {"value": f["value"], "ms_per_step": f["ms_max"] / args.steps,
+                            "bicgstab_iters_per_stage": round(f["iters"] / (3.0 * args.steps), 1),
+                            "roofline": f["roof"], "kernel_share": f["shares"], "gpu_launches": f["launches"],
+                            "clocks": f["clocks"]}
+        if cmp:
+            line["mixed_vs_fp64"] = cmp
         print(json.dumps(line), flush=True)
-    s.close()
+    for sv in solvers.values():
+        sv[0].close()
     if pg is not None:
         pg.destroy_process_group()
     return 0
@@ -345,6 +400,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"])
+    ap.add_argument("--profile-run", action="store_true",
+                    help="device-timed region only (no end-to-end leg, no CPU baseline), for ncu captures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

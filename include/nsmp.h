@@ -130,8 +130,10 @@ int nsmp_rk2_finalize(nsmp_ctx* ctx);        /* nsmp3D.F90:531-546 */
 /* u,v,w(n+1) = a*u(n) + b*u(n+1) over all cells (SSP-RK3 combinations). */
 int nsmp_rk_combine(nsmp_ctx* ctx, double a, double b);
 int nsmp_time_update(nsmp_ctx* ctx);         /* LoopTimeUpdate.F90:228-250 */
-/* Convenience: nsteps full steps; fin_rk 1 = Euler->AB2, 2 = RK2, 3 = SSP-RK3. */
-int nsmp_step(nsmp_ctx* ctx, int fin_rk, int nsteps, nsmp_stage_info* last);
+/* Convenience: nsteps full steps; fin_rk 1 = Euler->AB2, 2 = RK2, 3 = SSP-RK3.
+ * *flag_ab is read before the first stage and written after the last one
+ * (the switch of hydro.F90:469-478); NULL keeps the context's flag. */
+int nsmp_step(nsmp_ctx* ctx, int fin_rk, int nsteps, int* flag_ab, nsmp_stage_info* last);
 
 /* glob_cfl mass-flux reductions (cfl.F90:131-184), FP64 on the device:
  * out[0] = sum|div|, out[1] = max|div|, out[2] = sum div, out[3] = max CFL. */

@@ -1,0 +1,60 @@
+"""Mixed precision (NSMP_MIXED): FP32 inner BiCGSTAB inside FP64 iterative
+refinement.  The stopping test is the reference's, on the FP64 residual, so
+the mixed solution agrees with the FP64 one to the solver tolerance."""
+import numpy as np
+import pytest
+
+import nsmp_gb300 as ng
+from oracle import oracle_ctypes as oc
+from helpers import interior, oracle_params, rel_l2, small_case
+
+pytestmark = pytest.mark.gpu
+
+
+def _start(prm, mesh, seed=1):
+    s = ng.Solver(prm, mesh)
+    u, v, w, p = ng.initial_channel(prm, s.ncell, seed=seed)
+    s.user_initial(u, v, w, p)
+    return s, (u, v, w, p)
+
+
+def test_mixed_one_stage_vs_oracle():
+    """Refinement to 1e-13 reproduces the oracle's FP64 stage."""
+    prm, mesh = small_case(8, 6, layers=8, eps=1e-13, max_iters=5000, precision=ng.MIXED)
+    s, st = _start(prm, mesh)
+    o = oc.Oracle(oracle_params(prm), mesh)
+    o.user_initial(*st)
+    o.step(1)
+    rc, inf = s.step(1, 1)
+    assert rc == 0 and inf["converged"] == 1
+    assert min(inf["e1norm"], inf["e2norm"]) < 1e-13
+    for fg, fo in ((ng.F_U, oc.F_U), (ng.F_V, oc.F_V), (ng.F_W, oc.F_W)):
+        assert rel_l2(interior(s.download(fg), o.n0), interior(o.get(fo), o.n0)) <= 1e-10
+    assert rel_l2(interior(s.download(ng.F_P), o.n0), interior(o.get(oc.F_P), o.n0)) <= 1e-9
+
+
+def test_mixed_matches_fp64_after_steps():
+    """configs[0] mesh, 20 RK3 steps at eps = 1e-10: mixed vs FP64 GPU."""
+    prm, mesh = small_case(32, 16, layers=32, dt=1e-3)
+    s64, _ = _start(prm, mesh)
+    s32, _ = _start(dict(prm, precision=ng.MIXED), mesh)
+    for _ in range(20):
+        rc64, i64 = s64.step(3, 1)
+        rc32, i32 = s32.step(3, 1)
+        assert rc64 == 0 and rc32 == 0
+        assert i32["converged"] == 1 and min(i32["e1norm"], i32["e2norm"]) < 1e-10
+    for f in (ng.F_U, ng.F_V, ng.F_W):
+        assert rel_l2(interior(s32.download(f), prm["n0"]), interior(s64.download(f), prm["n0"])) <= 1e-6
+    d64, d32 = s64.mass_diag(), s32.mass_diag()
+    # divergence of the projected face fluxes: same to 1e-10 (relative to the flux scale)
+    assert abs(d32[1] - d64[1]) <= 1e-10 * max(1.0, d64[0])
+
+
+def test_set_precision_switch():
+    prm, mesh = small_case(8, 6, layers=6)
+    s, _ = _start(prm, mesh)
+    s.step(1, 1)
+    assert s.L.nsmp_set_precision(s.h, ng.MIXED) == 0
+    rc, inf = s.step(1, 1)
+    assert rc == 0 and inf["converged"] == 1
+    assert s.L.nsmp_set_precision(s.h, 7) == ng.ERR_ARG
