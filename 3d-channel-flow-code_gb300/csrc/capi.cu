@@ -1,5 +1,6 @@
 // C-ABI entry points (include/nsmp.h).  Every function catches host
 // exceptions and returns a status; nothing throws across the boundary.
+#include <algorithm>
 #include <cstring>
 #include <new>
 
@@ -235,6 +236,14 @@ int nsmp_set_precision(nsmp_ctx* c, int mode) {
     return NSMP_OK;
 }
 
+int nsmp_set_inner_solver(nsmp_ctx* c, double inner_tol, int inner_cap, int restart_every) {
+    if (!c || !(inner_tol > 0.0) || !(inner_tol < 1.0) || inner_cap < 1 || restart_every < 1) return NSMP_ERR_ARG;
+    c->inner_tol = inner_tol;
+    c->inner_cap = inner_cap;
+    c->restart_every = restart_every;
+    return NSMP_OK;
+}
+
 int nsmp_prof_enable(nsmp_ctx* c, int on) {
     if (!c) return NSMP_ERR_ARG;
     if (c->stream) cudaStreamSynchronize(c->stream);
@@ -252,6 +261,20 @@ int nsmp_prof_read(nsmp_ctx* c, int kid, long long* launches, double* total_ms) 
     *launches = c->prof_count[kid];
     *total_ms = c->prof_ms[kid];
     return NSMP_OK;
+}
+
+int nsmp_solver_log(nsmp_ctx* c, int max_cycles, int* inner_iters, double* inner_res, double* outer_res,
+                    int* accepted) {
+    if (!c || max_cycles < 0 || !inner_iters || !inner_res || !outer_res || !accepted) return NSMP_ERR_ARG;
+    const nsmp::Scal& s = *c->h_scal;
+    const int n = std::min(std::min(max_cycles, s.outer), nsmp::Scal::kCycLog);
+    for (int k = 0; k < n; ++k) {
+        inner_iters[k] = s.cyc_it[k];
+        inner_res[k] = s.cyc_in[k];
+        outer_res[k] = s.cyc_out[k];
+        accepted[k] = s.cyc_acc[k];
+    }
+    return n;
 }
 
 int nsmp_counters(nsmp_ctx* c, long long* launches, long long* bicg_iters) {

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -43,9 +44,10 @@ struct nsmp_ctx {
     float *r32 = nullptr, *r032 = nullptr, *p32[2] = {}, *v32[2] = {}, *s32 = nullptr, *t32 = nullptr,
           *e32 = nullptr, *invD32 = nullptr, *lev32 = nullptr;
     nsmp::ColPPE32* d_ppe32 = nullptr;
-    double inner_tol = 1e-4;
+    double inner_tol = 1e-1;      // FP32 residual reduction that triggers an FP64 update
+    int inner_cap = 50;           // most FP32 iterations between two FP64 updates
+    int restart_every = 300;      // most FP32 iterations of one Krylov process
     int last_outer = 0;
-    int last_inner_chunk = 16;
     double* stage_buf = nullptr;  // (N_CELL,NZ) staging for transfers
     // reductions and scalars
     nsmp::RedScratch red{}, red2{};
@@ -63,6 +65,7 @@ struct nsmp_ctx {
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
     std::vector<std::pair<int, int>> ev_pending;  // (kernel id, first event index)
+    std::map<const void*, int> occ_cache;  // kernel -> resident blocks per SM
     long long prof_count[NSMP_K_COUNT] = {};
     double prof_ms[NSMP_K_COUNT] = {};
 };
@@ -81,6 +84,10 @@ int run_mass_diag(nsmp_ctx* c, double out[4]);
 int run_download_pv(nsmp_ctx* c, double* host);
 int cuda_fail(nsmp_ctx* c, cudaError_t e, const char* where);
 int mixed_alloc(nsmp_ctx* c);
+int fp64_setup(nsmp_ctx* c);
+// FP64 pressure solve of one stage; on return *x_final points at the solution
+// (compact layout, before the Glob_Norm mean removal).
+int run_pressure_fp64(nsmp_ctx* c, const double* pf, const double** x_final);
 // Pressure solve of one stage in mixed precision; on return *x_final points
 // at the FP64 solution (before the Glob_Norm mean removal).
 int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final);

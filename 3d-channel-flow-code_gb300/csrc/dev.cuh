@@ -7,7 +7,7 @@
 namespace nsmp {
 
 constexpr int kBlock = 256;   // threads per block of every per-prism kernel
-constexpr int kMaxRed = 4;    // values reduced at once
+constexpr int kMaxRed = 5;    // values reduced at once
 
 // Per-layer factor rows of the level table (lev[row*NZ + k0]).
 enum LevRow {
@@ -26,10 +26,26 @@ struct Scal {
     int iter, done, converged, status;
     int max_iters, pad;
     double eps;
-    // mixed precision: inner FP32 BiCGSTAB state and outer refinement count
+    // mixed precision: FP32 BiCGSTAB with FP64 reliable updates
     double ib1, ib2, ir1, ir2, irho, irho_prev, ialpha, iomega, ir0v;
-    double inner_tol;
-    int iiter, idone, outer, pad2;
+    double inner_tol;      // reduction of the FP32 residual that triggers an FP64 update
+    double iscale;         // residual RMS at the start of the solve (FP32 values are r / iscale)
+    double r2_upd;         // FP64 |r|_2 at the last update
+    double rmean, emean;   // plain means of the FP64 residual and of the FP32 correction
+    int iiter;             // iterations since the last Krylov restart (0: p = r)
+    int ksince;            // iterations since the last FP64 update
+    int outer;             // FP64 updates done
+    int pending;           // 1: FP64 update requested
+    int restart;           // 1: restart the Krylov process at the next update
+    int efresh, has_e;     // correction accumulator state
+    int inner_cap;         // most FP32 iterations between two FP64 updates
+    int cur;               // buffer holding the current x and r
+    int restart_every;     // most FP32 iterations of one Krylov process
+    // per-update record of the last mixed solve (diagnostics)
+    static constexpr int kCycLog = 48;
+    int cyc_it[kCycLog];
+    float cyc_in[kCycLog], cyc_out[kCycLog];
+    int cyc_acc[kCycLog];
 };
 
 // Everything a kernel needs to address the mesh; passed by value.

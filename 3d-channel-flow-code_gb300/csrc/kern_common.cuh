@@ -22,6 +22,19 @@ __device__ __forceinline__ double ppe_row(const Mesh& m, const ColPPE& P, int k0
     return AA0 * x0 + AA1 * x1 + AA2 * x2 + AA3 * x3 + AAT * xT + AAB * xB;
 }
 
+// Compact interior layout of the solver vectors: index g = c*NZI + k0-1,
+// i.e. the prism's own thread index.  Neighbour column nb, same layer:
+// g + (nb - c)*NZI; vertical neighbours g +- 1 (inside the column).
+__device__ __forceinline__ size_t ICg(const Mesh& m, int c, int k0) { return (size_t)c * m.NZI + (k0 - 1); }
+
+// Cell-layout index of the prism with compact index g in column c.
+__device__ __forceinline__ size_t cell_of(int g, int c) { return (size_t)g + 2 * (size_t)c + 1; }
+
+// Blocks that fit on the device at once for a kernel (one full wave).
+int occupancy_grid(nsmp_ctx* c, const void* kernel, long long n);
+template <class K>
+inline int grid_occ(nsmp_ctx* c, K kernel, long long n) { return occupancy_grid(c, (const void*)kernel, n); }
+
 inline int grid_for(const nsmp_ctx* c, long long n) {
     long long b = (n + kBlock - 1) / kBlock;
     long long cap = (long long)c->num_sms * 8;

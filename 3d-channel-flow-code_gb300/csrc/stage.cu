@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(kBlock) k_faces_div(Mesh m, FaceArgs a, RedScr
                 src += (pb - pa) * G.dle2[j];
             }
             r = r - src * dsv;
-            a.rhsp[q] = r;
+            a.rhsp[g] = r;
             part[0] += r;
         }
     }
@@ -241,204 +241,13 @@ __global__ void __launch_bounds__(kBlock) k_faces_div(Mesh m, FaceArgs a, RedScr
     }
 }
 
-// Jacobi diagonal 1/Am0 (diag_precdt, bicgstab.F90:831-836), once at setup.
-__global__ void k_inv_diag(Mesh m, double* invD) {
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
-        int c, k0;
-        prism_of(m, g, c, k0);
-        const ColPPE& P = m.ppe[c];
-        const double dsv = lev(m, LV_DSV, k0);
-        const double AAB = P.area * lev(m, LV_IDSB, k0) * lev(m, LV_WB, k0);
-        const double AAT = P.area * lev(m, LV_IDST, k0) * lev(m, LV_WT, k0);
-        const double AA0 = -1.0 * (AAT + AAB + P.kA[0] * dsv + P.kA[1] * dsv + P.kA[2] * dsv);
-        invD[IX(m, c, k0)] = 1.0 / AA0;
-    }
-}
-
-struct KryArgs {
-    const double* rhsp;
-    const double* pf;
-    double *x, *r, *r0, *p, *v, *s, *t;
-    const double* invD;
-    const double* ah[5];   // Jacobi-scaled couplings: nb 1..3, top, bottom
-};
-
-// Glob_Norm(rhs, 1) + initial residual and norms (bicgstab.F90:107-109,
-// 403-451).  x = pf is the initial guess (hydro.F90:388-392).
-__global__ void __launch_bounds__(kBlock) k_bicg_init(Mesh m, KryArgs a, RedScratch rs, Scal* sc) {
-    const double avec = sc->sum_rhs / m.tv_lsig;
-    double part[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
-        int c, k0;
-        prism_of(m, g, c, k0);
-        const ColPPE& P = m.ppe[c];
-        const size_t q = IX(m, c, k0);
-        const double b = a.rhsp[q] - avec * P.area * lev(m, LV_HMEAN, k0);
-        const double x0 = a.pf[q];
-        const double Ax = ppe_row(m, P, k0, x0, a.pf[IX(m, P.nb[0], k0)], a.pf[IX(m, P.nb[1], k0)],
-                                  a.pf[IX(m, P.nb[2], k0)], a.pf[q + 1], a.pf[q - 1]);
-        const double r = b - Ax;
-        a.x[q] = x0;
-        a.r[q] = r;
-        a.r0[q] = r;
-        part[0] += b * b; part[1] += r * r; part[2] += fabs(b); part[3] += fabs(r);
-    }
-    double tot[4];
-    if (grid_reduce<4, false>(part, rs, tot) && threadIdx.x == 0) {
-        double b2 = sqrt(tot[0]), r2 = sqrt(tot[1]), b1 = tot[2], r1 = tot[3];
-        if (b2 == 0.0) b2 = 1.0;
-        if (b1 == 0.0) b1 = 1.0;
-        sc->b1 = b1; sc->b2 = b2; sc->r1 = r1; sc->r2 = r2;
-        sc->e1 = r1 / b1; sc->e2 = r2 / b2;
-        sc->rho = tot[1];
-        sc->rho_prev = 1.0; sc->alpha = 1.0; sc->omega = 1.0;
-        sc->iter = 0;
-        sc->status = 0;
-        sc->converged = 0;
-        sc->done = 0;
-        if (!(r2 == r2)) { sc->status = NSMP_ERR_NAN; sc->done = 1; }
-        else if (sc->e1 < sc->eps || sc->e2 < sc->eps) { sc->converged = 1; sc->done = 1; }
-    }
-}
-
-// update_pk (bicgstab.F90:726-773)
-__global__ void __launch_bounds__(kBlock) k_bicg_p(Mesh m, KryArgs a, const Scal* sc) {
-    if (sc->done) return;
-    const int it = sc->iter;
-    const double beta = (sc->rho / sc->rho_prev) * (sc->alpha / sc->omega), om = sc->omega;
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
-        int c, k0;
-        prism_of(m, g, c, k0);
-        const size_t q = IX(m, c, k0);
-        a.p[q] = (it == 0) ? a.r[q] : a.r[q] + beta * (a.p[q] - om * a.v[q]);
-    }
-}
-
-// out = A D^-1 in (diag_precdt then get_Apk, bicgstab.F90:831-836, 976-997)
-// with the Jacobi-scaled coefficients ahat_j = A_ij / A_jj precomputed once
-// (the diagonal of A D^-1 is 1), and the fused dot products.
-// MODE 0: v = A D^-1 p, dot (r0, v);  MODE 1: t = A D^-1 s, dots (t, s), (t, t).
-template <int MODE>
-__global__ void __launch_bounds__(kBlock) k_bicg_spmv(Mesh m, KryArgs a, RedScratch rs, Scal* sc) {
-    if (sc->done) return;
-    const double* in = (MODE == 0) ? a.p : a.s;
-    double* out = (MODE == 0) ? a.v : a.t;
-    double part[2] = {0.0, 0.0};
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
-        int c, k0;
-        prism_of(m, g, c, k0);
-        const ColPPE& P = m.ppe[c];
-        const size_t q = IX(m, c, k0);
-        const double x0 = in[q];
-        double o = x0;
-        o = fma(a.ah[0][q], in[IX(m, P.nb[0], k0)], o);
-        o = fma(a.ah[1][q], in[IX(m, P.nb[1], k0)], o);
-        o = fma(a.ah[2][q], in[IX(m, P.nb[2], k0)], o);
-        // wall layers carry zero coefficients (AmB(i,2) = AmT(i,NZ-1) = 0)
-        o = fma(a.ah[3][q], in[q + 1], o);
-        o = fma(a.ah[4][q], in[q - 1], o);
-        out[q] = o;
-        if (MODE == 0) {
-            part[0] = fma(a.r0[q], o, part[0]);
-        } else {
-            part[0] = fma(o, x0, part[0]);
-            part[1] = fma(o, o, part[1]);
-        }
-    }
-    double tot[2];
-    if (MODE == 0) {
-        double p1[1] = {part[0]}, t1[1];
-        if (grid_reduce<1, false>(p1, rs, t1) && threadIdx.x == 0) {
-            sc->r0v = t1[0];
-            if (fabs(t1[0]) < 1.0e-30) { sc->done = 1; sc->status = NSMP_WARN_BREAKDOWN; }
-            else sc->alpha = sc->rho / t1[0];
-        }
-    } else {
-        if (grid_reduce<2, false>(part, rs, tot) && threadIdx.x == 0) {
-            sc->ts = tot[0];
-            sc->tt = tot[1];
-            sc->omega = tot[0] / tot[1];
-        }
-    }
-}
-
-// Scaled coefficients ahat = A_ij * (1/A_jj) of the five off-diagonal
-// couplings, once at setup; zero at the walls.
-__global__ void k_scaled_coefs(Mesh m, const double* __restrict__ invD, double* a1, double* a2, double* a3,
-                               double* aT, double* aB) {
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
-        int c, k0;
-        prism_of(m, g, c, k0);
-        const ColPPE& P = m.ppe[c];
-        const size_t q = IX(m, c, k0);
-        const double dsv = lev(m, LV_DSV, k0);
-        a1[q] = (P.kA[0] * dsv) * invD[IX(m, P.nb[0], k0)];
-        a2[q] = (P.kA[1] * dsv) * invD[IX(m, P.nb[1], k0)];
-        a3[q] = (P.kA[2] * dsv) * invD[IX(m, P.nb[2], k0)];
-        aT[q] = (k0 < m.NZ - 2) ? (P.area * lev(m, LV_IDST, k0)) * invD[q + 1] : 0.0;
-        aB[q] = (k0 > 1) ? (P.area * lev(m, LV_IDSB, k0)) * invD[q - 1] : 0.0;
-    }
-}
-
-// update_sk (bicgstab.F90:1007-1041)
-__global__ void __launch_bounds__(kBlock) k_bicg_s(Mesh m, KryArgs a, const Scal* sc) {
-    if (sc->done) return;
-    const double al = sc->alpha;
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
-        int c, k0;
-        prism_of(m, g, c, k0);
-        const size_t q = IX(m, c, k0);
-        a.s[q] = a.r[q] - al * a.v[q];
-    }
-}
-
-// update_xkrk (bicgstab.F90:1047-1111) + the next rho = (r0, r) and the
-// stopping test of bicgstab.F90:543-566.
-__global__ void __launch_bounds__(kBlock) k_bicg_x(Mesh m, KryArgs a, RedScratch rs, Scal* sc) {
-    if (sc->done) return;
-    const double al = sc->alpha, om = sc->omega;
-    double part[3] = {0.0, 0.0, 0.0};
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
-        int c, k0;
-        prism_of(m, g, c, k0);
-        const size_t q = IX(m, c, k0);
-        const double id = a.invD[q];
-        const double xn = fma(id, fma(om, a.s[q], al * a.p[q]), a.x[q]);
-        const double res = a.s[q] - om * a.t[q];
-        a.x[q] = xn;
-        a.r[q] = res;
-        part[0] += res * res;
-        part[1] += fabs(res);
-        part[2] += a.r0[q] * res;
-    }
-    double tot[3];
-    if (grid_reduce<3, false>(part, rs, tot) && threadIdx.x == 0) {
-        const double r2 = sqrt(tot[0]), r1 = tot[1];
-        sc->r1 = r1; sc->r2 = r2;
-        sc->e2 = r2 / sc->b2;
-        sc->e1 = r1 / sc->b1;
-        sc->rho_prev = sc->rho;
-        sc->rho = tot[2];
-        sc->iter = sc->iter + 1;
-        double en = 1.0e10;
-        if (en > sc->e1) en = sc->e1;
-        if (en > sc->e2) en = sc->e2;
-        if (!(r2 == r2)) { sc->status = NSMP_ERR_NAN; sc->done = 1; }
-        else if (en < sc->eps) { sc->converged = 1; sc->done = 1; }
-        else if (sc->iter > sc->max_iters) { sc->status = NSMP_WARN_MAXITER; sc->done = 1; }
-        else if (fabs(sc->rho_prev) < 1.0e-30 || fabs(sc->omega) < 1.0e-30) {
-            sc->status = NSMP_WARN_BREAKDOWN; sc->done = 1;
-        }
-    }
-}
-
 // Glob_Norm(phi, 0) sum (bicgstab.F90:617-640)
 __global__ void __launch_bounds__(kBlock) k_pmean(Mesh m, const double* __restrict__ x, RedScratch rs, Scal* sc) {
     double part[1] = {0.0};
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
         int c, k0;
         prism_of(m, g, c, k0);
-        part[0] += x[IX(m, c, k0)] * (m.ppe[c].area * lev(m, LV_HMEAN, k0));
+        part[0] += x[g] * (m.ppe[c].area * lev(m, LV_HMEAN, k0));
     }
     double tot[1];
     if (grid_reduce<1, false>(part, rs, tot) && threadIdx.x == 0) sc->avec_p = tot[0] / m.tv_lsig;
@@ -451,7 +260,7 @@ __global__ void k_vertex1(Mesh m, const double* __restrict__ x, const Scal* sc, 
         const int v = g / m.NZI, k0 = 1 + (g - v * m.NZI);
         double acc = 0.0;
         const int s1 = __ldg(m.vptr + v + 1);
-        for (int s = __ldg(m.vptr + v); s < s1; ++s) acc += __ldg(m.vcoef + s) * (x[IX(m, __ldg(m.vcell + s), k0)] - sh);
+        for (int s = __ldg(m.vptr + v); s < s1; ++s) acc += __ldg(m.vcoef + s) * (x[ICg(m, __ldg(m.vcell + s), k0)] - sh);
         pv[IV(m, v, k0)] = acc;
     }
 }
@@ -474,14 +283,14 @@ __global__ void __launch_bounds__(kBlock) k_project(Mesh m, ProjArgs a, const Sc
         prism_of(m, g, c, k0);
         const ColGeo& G = m.geo[c];
         const size_t q = IX(m, c, k0);
-        const double p = a.x[q] - avec;
+        const double p = a.x[g] - avec;
         // wall ghost layers of p are Neumann copies (BCpcenter, BC.F90:869-888)
-        const double pT = (k0 < m.NZ - 2) ? a.x[q + 1] - avec : p;
-        const double pB = (k0 > 1) ? a.x[q - 1] - avec : p;
+        const double pT = (k0 < m.NZ - 2) ? a.x[g + 1] - avec : p;
+        const double pB = (k0 > 1) ? a.x[g - 1] - avec : p;
         double dpdx = 0.0, dpdy = 0.0, dn[3];
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const double pn = a.x[IX(m, G.nb[j], k0)] - avec;
+            const double pn = a.x[ICg(m, G.nb[j], k0)] - avec;
             const double d = pn - p;
             dpdx += G.gx[j] * d;
             dpdy += G.gy[j] * d;
@@ -598,6 +407,24 @@ int cuda_fail(nsmp_ctx* c, cudaError_t e, const char* where) {
     return NSMP_ERR_CUDA;
 }
 
+int occupancy_grid(nsmp_ctx* c, const void* kernel, long long n) {
+    int per_sm = 0;
+    auto it = c->occ_cache.find(kernel);
+    if (it != c->occ_cache.end()) {
+        per_sm = it->second;
+    } else {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        if (per_sm > 8) per_sm = 8;  // reduction scratch holds 8 blocks per SM
+        c->occ_cache[kernel] = per_sm;
+    }
+    long long b = (n + kBlock - 1) / kBlock;
+    const long long cap = (long long)c->num_sms * per_sm;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
 int prof_begin(nsmp_ctx* c, int kid) {
     if (!c->prof_on) return -1;
     if (c->ev_used + 2 > c->ev_pool.size()) {
@@ -674,9 +501,7 @@ int run_stage(nsmp_ctx* c, int fin_rk, nsmp_stage_info* info) {
     c->lnp = np;
     double** K = c->lvl[c->lknown];
     double** N = c->lvl[np];
-    const int gp = grid_for(c, m.nprism);
-    const int gv = grid_for(c, (long long)m.nclass * m.NZI);
-    LAUNCH(NSMP_K_VERTEX4, k_vertex<4><<<gv, kBlock, 0, st>>>(m, K[0], K[1], K[2], K[3], c->vtx[0], c->vtx[1], c->vtx[2], c->vtx[3], 0.0));
+    LAUNCH(NSMP_K_VERTEX4, k_vertex<4><<<grid_occ(c, k_vertex<4>, (long long)m.nclass * m.NZI), kBlock, 0, st>>>(m, K[0], K[1], K[2], K[3], c->vtx[0], c->vtx[1], c->vtx[2], c->vtx[3], 0.0));
     CKL("k_vertex4");
     StageArgs sa;
     sa.u = K[0]; sa.v = K[1]; sa.w = K[2];
@@ -689,53 +514,22 @@ int run_stage(nsmp_ctx* c, int fin_rk, nsmp_stage_info* info) {
     sa.c2 = (c->flag_ab == 1) ? -0.55 : 0.0;
     sa.dt = P.dt; sa.inv_re = 1.0 / P.re; sa.bdx = P.bdx; sa.bdy = P.bdy; sa.bdz = P.bdz;
     sa.les = P.les; sa.les_van = P.les_van;
-    LAUNCH(NSMP_K_STAGE_RHS, k_stage_rhs<<<gp, kBlock, 0, st>>>(m, sa, c->red, c->d_scal));
+    LAUNCH(NSMP_K_STAGE_RHS, k_stage_rhs<<<grid_occ(c, k_stage_rhs, m.nprism), kBlock, 0, st>>>(m, sa, c->red, c->d_scal));
     CKL("k_stage_rhs");
     FaceArgs fa{c->ustar[0], c->ustar[1], c->ustar[2], c->vtx[3], c->face[0], c->face[1], c->face[2],
                 c->face[3], c->face[4], c->rhsp, 1.0 / P.dt, 1};
-    LAUNCH(NSMP_K_FACES_DIV, k_faces_div<<<gp, kBlock, 0, st>>>(m, fa, c->red, c->d_scal));
+    LAUNCH(NSMP_K_FACES_DIV, k_faces_div<<<grid_occ(c, k_faces_div, m.nprism), kBlock, 0, st>>>(m, fa, c->red, c->d_scal));
     CKL("k_faces_div");
-    const double* xsol = c->x;
-    if (c->precision == NSMP_MIXED) {
-        int rc = run_pressure_mixed(c, K[3], &xsol);
-        if (rc) return rc;
-    } else {
-        KryArgs ka{c->rhsp, K[3], c->x, c->r, c->r0, c->pk, c->vk, c->sk, c->tk, c->invD,
-                   {c->ahat[0], c->ahat[1], c->ahat[2], c->ahat[3], c->ahat[4]}};
-        LAUNCH(NSMP_K_BICG_INIT, k_bicg_init<<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
-        CKL("k_bicg_init");
-        // BiCGSTAB iterations, enqueued in chunks; every kernel returns at once
-        // after the device-side stopping test has fired.
-        int chunk = c->last_iters > 2 ? c->last_iters - 1 : 2;
-        int launched = 0;
-        for (;;) {
-            for (int it = 0; it < chunk; ++it) {
-                LAUNCH(NSMP_K_BICG_P, k_bicg_p<<<gp, kBlock, 0, st>>>(m, ka, c->d_scal));
-                LAUNCH(NSMP_K_BICG_SPMV_V, k_bicg_spmv<0><<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
-                LAUNCH(NSMP_K_BICG_S, k_bicg_s<<<gp, kBlock, 0, st>>>(m, ka, c->d_scal));
-                LAUNCH(NSMP_K_BICG_SPMV_T, k_bicg_spmv<1><<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
-                LAUNCH(NSMP_K_BICG_X, k_bicg_x<<<gp, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
-            }
-            CKL("bicgstab iteration");
-            launched += chunk;
-            CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
-            prof_resolve(c);
-            if (c->h_scal->done) break;
-            if (launched > P.max_iters + 8) {  // cannot happen: the device test stops at MaxIters
-                c->err = "BiCGSTAB did not stop";
-                return NSMP_ERR_CUDA;
-            }
-            chunk = 4;
-        }
-    }
-    LAUNCH(NSMP_K_PMEAN, k_pmean<<<gp, kBlock, 0, st>>>(m, xsol, c->red, c->d_scal));
+    const double* xsol = nullptr;
+    const int rcp = (c->precision == NSMP_MIXED) ? run_pressure_mixed(c, K[3], &xsol) : run_pressure_fp64(c, K[3], &xsol);
+    if (rcp) return rcp;
+    LAUNCH(NSMP_K_PMEAN, k_pmean<<<grid_occ(c, k_pmean, m.nprism), kBlock, 0, st>>>(m, xsol, c->red, c->d_scal));
     CKL("k_pmean");
-    LAUNCH(NSMP_K_VERTEX1, k_vertex1<<<gv, kBlock, 0, st>>>(m, xsol, c->d_scal, c->vtx[3]));
+    LAUNCH(NSMP_K_VERTEX1, k_vertex1<<<grid_occ(c, k_vertex1, (long long)m.nclass * m.NZI), kBlock, 0, st>>>(m, xsol, c->d_scal, c->vtx[3]));
     CKL("k_vertex1");
     ProjArgs pa{xsol, c->vtx[3], c->ustar[0], c->ustar[1], c->ustar[2], c->face[0], c->face[1], c->face[2],
                 c->face[3], c->face[4], N[0], N[1], N[2], N[3], P.dt};
-    LAUNCH(NSMP_K_PROJECT, k_project<<<gp, kBlock, 0, st>>>(m, pa, c->d_scal));
+    LAUNCH(NSMP_K_PROJECT, k_project<<<grid_occ(c, k_project, m.nprism), kBlock, 0, st>>>(m, pa, c->d_scal));
     CKL("k_project");
     CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -750,7 +544,17 @@ int run_stage(nsmp_ctx* c, int fin_rk, nsmp_stage_info* info) {
     inf.converged = s.converged;
     inf.max_eddy = P.les ? s.max_eddy : 0.0;
     inf.status = s.status;
+    inf.refinements = (c->precision == NSMP_MIXED) ? s.outer : 0;
     c->last = inf;
+    if (s.status == NSMP_ERR_NAN) {
+        char buf[512];
+        snprintf(buf, sizeof buf,
+                 "non-finite residual: iter %d inner %d refinements %d | rho %.3e rho_prev %.3e alpha %.3e "
+                 "omega %.3e r0v %.3e | inner r1 %.3e r2 %.3e b1 %.3e b2 %.3e | outer e1 %.3e e2 %.3e",
+                 s.iter, s.iiter, s.outer, s.irho, s.irho_prev, s.ialpha, s.iomega, s.ir0v, s.ir1, s.ir2, s.ib1,
+                 s.ib2, s.e1, s.e2);
+        c->err = buf;
+    }
     if (info) *info = inf;
     if (fin_rk == 1 && c->flag_ab != 1) c->flag_ab = 1;  // hydro.F90:469-478
     return s.status;
@@ -879,11 +683,10 @@ int ctx_init_device(nsmp_ctx* c) {
     m.lev = c->d_lev;
     for (int q = 0; q < 3; ++q) { m.sgn_bot[q] = L.sgn_bot[q]; m.sgn_top[q] = L.sgn_top[q]; }
     m.tv_lsig = L.total_volume * L.lsig;
-    k_inv_diag<<<grid_for(c, m.nprism), kBlock, 0, c->stream>>>(m, c->invD);
-    CKL("k_inv_diag");
-    k_scaled_coefs<<<grid_for(c, m.nprism), kBlock, 0, c->stream>>>(m, c->invD, c->ahat[0], c->ahat[1], c->ahat[2],
-                                                                   c->ahat[3], c->ahat[4]);
-    CKL("k_scaled_coefs");
+    {
+        int rc = fp64_setup(c);
+        if (rc) return rc;
+    }
     Scal s0{};
     s0.eps = c->prm.eps;
     s0.max_iters = c->prm.max_iters;

@@ -48,7 +48,8 @@ class Mesh(C.Structure):
 
 class StageInfo(C.Structure):
     _fields_ = [("iters", C.c_int), ("e1norm", C.c_double), ("e2norm", C.c_double),
-                ("converged", C.c_int), ("max_eddy", C.c_double), ("status", C.c_int)]
+                ("converged", C.c_int), ("max_eddy", C.c_double), ("status", C.c_int),
+                ("refinements", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -60,6 +61,7 @@ EXPORTS = [
     "nsmp_rk2_finalize", "nsmp_rk_combine", "nsmp_time_update", "nsmp_step", "nsmp_mass_diag",
     "nsmp_set_precision", "nsmp_stream", "nsmp_mesh_size", "nsmp_mesh_generate", "nsmp_initial_channel",
     "nsmp_sigma_grid", "nsmp_geometry", "nsmp_prof_enable", "nsmp_prof_read", "nsmp_counters",
+    "nsmp_set_inner_solver", "nsmp_solver_log",
 ]
 
 (K_VERTEX4, K_STAGE_RHS, K_FACES_DIV, K_BICG_INIT, K_BICG_P, K_BICG_SPMV_V, K_BICG_S, K_BICG_SPMV_T,
@@ -102,6 +104,7 @@ def lib(build_if_missing=True):
     L.nsmp_step.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(StageInfo)]
     L.nsmp_mass_diag.argtypes = [vp, vp]
     L.nsmp_set_precision.argtypes = [vp, C.c_int]
+    L.nsmp_set_inner_solver.argtypes = [vp, C.c_double, C.c_int, C.c_int]
     L.nsmp_stream.argtypes = [vp]
     L.nsmp_stream.restype = vp
     L.nsmp_mesh_size.argtypes = [C.c_int, C.c_int, P(C.c_int), P(C.c_int)]
@@ -113,6 +116,7 @@ def lib(build_if_missing=True):
     L.nsmp_prof_enable.argtypes = [vp, C.c_int]
     L.nsmp_prof_read.argtypes = [vp, C.c_int, P(C.c_longlong), P(C.c_double)]
     L.nsmp_counters.argtypes = [vp, P(C.c_longlong), P(C.c_longlong)]
+    L.nsmp_solver_log.argtypes = [vp, C.c_int, vp, vp, vp, vp]
     _lib = L
     return L
 
@@ -291,6 +295,12 @@ class Solver:
     def stream(self):
         return self.L.nsmp_stream(self.h)
 
+    def set_precision(self, mode):
+        self._check(self.L.nsmp_set_precision(self.h, int(mode)))
+
+    def set_inner_solver(self, inner_tol=1e-1, inner_cap=50, restart_every=300):
+        self._check(self.L.nsmp_set_inner_solver(self.h, float(inner_tol), int(inner_cap), int(restart_every)))
+
     def prof_enable(self, on=True):
         self._check(self.L.nsmp_prof_enable(self.h, 1 if on else 0))
 
@@ -302,6 +312,16 @@ class Solver:
             self._check(self.L.nsmp_prof_read(self.h, k, C.byref(n), C.byref(ms)))
             out[KERNEL_NAMES[k]] = (n.value, ms.value)
         return out
+
+    def solver_log(self):
+        """Per refinement cycle of the last mixed solve: (inner its, inner res, outer res, accepted)."""
+        n = 48
+        it = np.zeros(n, np.int32)
+        ri = np.zeros(n)
+        ro = np.zeros(n)
+        ac = np.zeros(n, np.int32)
+        k = self._check(self.L.nsmp_solver_log(self.h, n, _p(it), _p(ri), _p(ro), _p(ac)))
+        return list(zip(it[:k].tolist(), ri[:k].tolist(), ro[:k].tolist(), ac[:k].tolist()))
 
     def counters(self):
         """(kernel launches, BiCGSTAB iterations) since creation."""

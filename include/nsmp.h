@@ -79,6 +79,7 @@ typedef struct nsmp_stage_info {
     int converged;     /* 1 if min(e1norm, e2norm) < eps                        */
     double max_eddy;   /* max nu_t (0 without LES)                              */
     int status;        /* status of the stage                                   */
+    int refinements;   /* NSMP_MIXED: FP64 refinement cycles (0 in NSMP_FP64)   */
 } nsmp_stage_info;
 
 typedef struct nsmp_ctx nsmp_ctx;
@@ -139,6 +140,15 @@ int nsmp_step(nsmp_ctx* ctx, int fin_rk, int nsteps, int* flag_ab, nsmp_stage_in
  * out[0] = sum|div|, out[1] = max|div|, out[2] = sum div, out[3] = max CFL. */
 int nsmp_mass_diag(nsmp_ctx* ctx, double out[4]);
 int nsmp_set_precision(nsmp_ctx* ctx, int mode);
+/* NSMP_MIXED pressure solver.  The FP32 BiCGSTAB hands its correction to
+ * FP64 (x += e, r = b - A x, the FP32 residual replaced by the FP64 one) when
+ * its residual fell by inner_tol since the last hand-over (default 1e-1) or
+ * after inner_cap iterations (default 50), and restarts its Krylov process
+ * after restart_every iterations (default 300) or when a hand-over did not
+ * lower the FP64 residual.  The FP64 stopping test (eps) is unaffected: these
+ * trade hand-overs against iterations, not accuracy.  The mixed mode needs an
+ * even number of interior layers. */
+int nsmp_set_inner_solver(nsmp_ctx* ctx, double inner_tol, int inner_cap, int restart_every);
 /* Stream used by the context (cudaStream_t as void*). */
 void* nsmp_stream(nsmp_ctx* ctx);
 
@@ -155,6 +165,12 @@ enum {
  * Enabling also clears the accumulators. */
 int nsmp_prof_enable(nsmp_ctx* ctx, int on);
 int nsmp_prof_read(nsmp_ctx* ctx, int kernel_id, long long* launches, double* total_ms);
+/* NSMP_MIXED diagnostics of the last stage's pressure solve: per FP64
+ * refinement cycle the FP32 inner iterations, the inner relative residual
+ * reached, the FP64 relative residual after the cycle and whether the cycle
+ * was accepted.  Returns the number of cycles written (at most 48). */
+int nsmp_solver_log(nsmp_ctx* ctx, int max_cycles, int* inner_iters, double* inner_res,
+                    double* outer_res, int* accepted);
 /* Kernels launched and BiCGSTAB iterations executed since creation. */
 int nsmp_counters(nsmp_ctx* ctx, long long* launches, long long* bicg_iters);
 
