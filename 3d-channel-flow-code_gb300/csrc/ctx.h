@@ -81,6 +81,7 @@ int run_combine(nsmp_ctx* c, double a, double b);
 int run_gather(nsmp_ctx* c, const double* dfield, int ghost_mode, int rows, double* host);
 int run_scatter(nsmp_ctx* c, const double* host, double* dfield);
 int run_mass_diag(nsmp_ctx* c, double out[4]);
+int run_mass_diag_noalloc(nsmp_ctx* c, double out[4]);
 int run_download_pv(nsmp_ctx* c, double* host);
 int cuda_fail(nsmp_ctx* c, cudaError_t e, const char* where);
 int mixed_alloc(nsmp_ctx* c);

@@ -61,7 +61,7 @@ EXPORTS = [
     "nsmp_rk2_finalize", "nsmp_rk_combine", "nsmp_time_update", "nsmp_step", "nsmp_mass_diag",
     "nsmp_set_precision", "nsmp_stream", "nsmp_mesh_size", "nsmp_mesh_generate", "nsmp_initial_channel",
     "nsmp_sigma_grid", "nsmp_geometry", "nsmp_prof_enable", "nsmp_prof_read", "nsmp_counters",
-    "nsmp_set_inner_solver", "nsmp_solver_log",
+    "nsmp_set_inner_solver", "nsmp_solver_log", "nsmp_mass_diag_noalloc",
 ]
 
 (K_VERTEX4, K_STAGE_RHS, K_FACES_DIV, K_BICG_INIT, K_BICG_P, K_BICG_SPMV_V, K_BICG_S, K_BICG_SPMV_T,
@@ -103,6 +103,7 @@ def lib(build_if_missing=True):
     L.nsmp_rk_combine.argtypes = [vp, C.c_double, C.c_double]
     L.nsmp_step.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(StageInfo)]
     L.nsmp_mass_diag.argtypes = [vp, vp]
+    L.nsmp_mass_diag_noalloc.argtypes = [vp, vp]
     L.nsmp_set_precision.argtypes = [vp, C.c_int]
     L.nsmp_set_inner_solver.argtypes = [vp, C.c_double, C.c_int, C.c_int]
     L.nsmp_stream.argtypes = [vp]
@@ -289,6 +290,12 @@ class Solver:
     def mass_diag(self):
         out = np.zeros(4, dtype=np.float64)
         self._check(self.L.nsmp_mass_diag(self.h, _p(out)))
+        return out
+
+    def mass_diag_noalloc(self):
+        """nsmp_mass_diag_noalloc: the same reductions with no allocation."""
+        out = np.zeros(4, dtype=np.float64)
+        self._check(self.L.nsmp_mass_diag_noalloc(self.h, _p(out)))
         return out
 
     @property

@@ -140,6 +140,18 @@ int nsmp_step(nsmp_ctx* ctx, int fin_rk, int nsteps, int* flag_ab, nsmp_stage_in
  * out[0] = sum|div|, out[1] = max|div|, out[2] = sum div, out[3] = max CFL. */
 int nsmp_mass_diag(nsmp_ctx* ctx, double out[4]);
 int nsmp_set_precision(nsmp_ctx* ctx, int mode);
+/* The reductions of nsmp_mass_diag without any allocation (no counterpart in
+ * the reference).  For callers that cannot allocate device memory after
+ * setup -- a driver that reserves a fixed device-memory budget before its
+ * time loop, or one that forbids allocation inside the loop because it can
+ * synchronise the device -- the reduction scratch lives in a static device
+ * array of the library instead of in context buffers.  Limit: contexts of at
+ * most 16,777,216 prisms (65536 blocks of 256); larger ones get
+ * NSMP_ERR_RANGE.  The array (about 2 MB) stays on every GPU that loaded the
+ * library until exit.  All calls share it, so calls that overlap on the GPU
+ * race; the first call on a device resolves the array's address and should
+ * come before any stream capture. */
+int nsmp_mass_diag_noalloc(nsmp_ctx* ctx, double out[4]);
 /* NSMP_MIXED pressure solver.  The FP32 BiCGSTAB hands its correction to
  * FP64 (x += e, r = b - A x, the FP32 residual replaced by the FP64 one) when
  * its residual fell by inner_tol since the last hand-over (default 1e-1) or
