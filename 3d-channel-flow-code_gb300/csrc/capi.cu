@@ -268,11 +268,12 @@ int nsmp_solver_log(nsmp_ctx* c, int max_cycles, int* inner_iters, double* inner
     if (!c || max_cycles < 0 || !inner_iters || !inner_res || !outer_res || !accepted) return NSMP_ERR_ARG;
     const nsmp::Scal& s = *c->h_scal;
     const int n = std::min(std::min(max_cycles, s.outer), nsmp::Scal::kCycLog);
-    for (int k = 0; k < n; ++k) {
-        inner_iters[k] = s.cyc_it[k];
-        inner_res[k] = s.cyc_in[k];
-        outer_res[k] = s.cyc_out[k];
-        accepted[k] = s.cyc_acc[k];
+    for (int k = 0; k < n; ++k) {  // the last n updates, oldest first
+        const int q = (s.outer - n + k) % nsmp::Scal::kCycLog;
+        inner_iters[k] = s.cyc_it[q];
+        inner_res[k] = s.cyc_in[q];
+        outer_res[k] = s.cyc_out[q];
+        accepted[k] = s.cyc_acc[q];
     }
     return n;
 }

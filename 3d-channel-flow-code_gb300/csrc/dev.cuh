@@ -7,7 +7,7 @@
 namespace nsmp {
 
 constexpr int kBlock = 256;   // threads per block of every per-prism kernel
-constexpr int kMaxRed = 5;    // values reduced at once
+constexpr int kMaxRed = 8;    // values reduced at once
 
 // Per-layer factor rows of the level table (lev[row*NZ + k0]).
 enum LevRow {
@@ -30,14 +30,19 @@ struct Scal {
     double ib1, ib2, ir1, ir2, irho, irho_prev, ialpha, iomega, ir0v;
     double inner_tol;      // reduction of the FP32 residual that triggers an FP64 update
     double iscale;         // residual RMS at the start of the solve (FP32 values are r / iscale)
-    double r2_upd;         // FP64 |r|_2 at the last update
+    double theta;          // minimal-residual step of the last FP64 update
+    double r2sq, rsum;     // |r|_2^2 and sum of the current FP64 residual
     double rmean, emean;   // plain means of the FP64 residual and of the FP32 correction
+    double ise, isy;       // sum of e and of D^-1 p formed by the p/v pass
     int iiter;             // iterations since the last Krylov restart (0: p = r)
     int ksince;            // iterations since the last FP64 update
     int outer;             // FP64 updates done
     int pending;           // 1: FP64 update requested
     int restart;           // 1: restart the Krylov process at the next update
-    int efresh, has_e;     // correction accumulator state
+    int perturb;           // 1: perturb the shadow residual at that restart
+    int has_e;             // 1: e holds a correction
+    int einc;              // 1: e lacks D^-1 (alpha p + omega s) of the last iteration
+    int rfresh;            // 1: r was set by an FP64 update (else r = s - omega t)
     int inner_cap;         // most FP32 iterations between two FP64 updates
     int cur;               // buffer holding the current x and r
     int restart_every;     // most FP32 iterations of one Krylov process
@@ -113,13 +118,13 @@ __device__ __forceinline__ void block_reduce(double (&x)[N]) {
     __syncthreads();
 }
 
-// Grid reduction: every block contributes x; the last block to arrive gets
-// the totals in `tot` (all its threads) and returns true.  The counter is
-// reset by the last block so the scratch is reusable by the next launch.
+// Last-block part of a grid reduction: x (valid in thread 0) is this block's
+// contribution; the last block to arrive gets the totals in `tot` (all its
+// threads) and returns true.  The counter is reset by the last block so the
+// scratch is reusable by the next launch.
 template <int N, bool MAX>
-__device__ bool grid_reduce(double (&x)[N], RedScratch rs, double (&tot)[N]) {
+__device__ bool grid_finish(const double (&x)[N], RedScratch rs, double (&tot)[N]) {
     __shared__ bool last;
-    block_reduce<N, MAX>(x);
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int q = 0; q < N; ++q) rs.partials[blockIdx.x * kMaxRed + q] = x[q];
@@ -150,6 +155,47 @@ __device__ bool grid_reduce(double (&x)[N], RedScratch rs, double (&tot)[N]) {
 #pragma unroll
     for (int q = 0; q < N; ++q) tot[q] = res[q];
     return true;
+}
+
+// Grid reduction of FP64 values (sum or max), fixed order: deterministic for
+// a fixed grid.
+template <int N, bool MAX>
+__device__ bool grid_reduce(double (&x)[N], RedScratch rs, double (&tot)[N]) {
+    block_reduce<N, MAX>(x);
+    return grid_finish<N, MAX>(x, rs, tot);
+}
+
+// Grid sum of FP32 per-thread values: FP32 inside each warp (a 32-value tree,
+// relative error at most 5 units of FP32 rounding), FP64 across warps and
+// blocks.  Used by the FP32 inner solver, whose values are formed in FP32
+// anyway; it keeps FP64 instructions (a few per SM cycle on this GPU) out of
+// the bandwidth-bound passes.
+template <int N>
+__device__ bool grid_reduce_f(float (&x)[N], RedScratch rs, double (&tot)[N]) {
+    __shared__ double sh[kBlock / 32][N];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+        float y = x[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) y += __shfl_down_sync(0xffffffffu, y, o);
+        if (lane == 0) sh[wid][q] = (double)y;
+    }
+    __syncthreads();
+    double d[N];
+#pragma unroll
+    for (int q = 0; q < N; ++q) d[q] = 0.0;
+    if (wid == 0) {
+#pragma unroll
+        for (int q = 0; q < N; ++q) {
+            double y = (lane < kBlock / 32) ? sh[lane][q] : 0.0;
+#pragma unroll
+            for (int o = kBlock / 64; o > 0; o >>= 1) y += __shfl_down_sync(0xffffffffu, y, o);
+            d[q] = y;
+        }
+    }
+    __syncthreads();
+    return grid_finish<N, false>(d, rs, tot);
 }
 
 }  // namespace nsmp

@@ -7,11 +7,13 @@
 // wrapped in FP64 iterative refinement by reliable updates (Sleijpen and
 // van der Vorst 1996; Clark et al. 2010 for mixed precision):
 //
-//   FP32 BiCGSTAB iterations on A e = r, e accumulated     k_in_pv / k_in_st / k_in_upd
+//   FP32 BiCGSTAB iterations on A e = r, e accumulated     k_in_pv / k_in_st
 //   when the FP32 residual fell by inner_tol (or after
 //   inner_cap iterations):
-//     x = x + e,  r = b - A x          FP64, FP64 norms     k_mix_update
-//     FP32 r <- r (true residual)       Krylov state kept   k_mix_scale
+//     x1 = x + e, r1 = b - A x1         FP64                 k_mix_update
+//     x, r <- x + theta (x1 - x), r + theta (r1 - r) with the minimal-residual
+//     theta; stopping test on the FP64 norms               k_mix_scale
+//     FP32 r <- r (true residual)       Krylov state kept   k_mix_scale/_shadow
 //
 // Replacing the drifting FP32 recursive residual by the FP64 truth, while
 // keeping p, v, the shadow residual and rho, lets one Krylov process run to
@@ -26,9 +28,10 @@
 // plain mean removed and e is added with its mean removed (the pressure level
 // is fixed afterwards by Glob_Norm anyway).
 //
-// The two stencil passes fuse the p and s vector updates (evaluated at the
-// seven stencil points); dot products are formed per thread in FP32 over the
-// thread's few prisms and reduced across threads and blocks in FP64.
+// An iteration is two stencil passes that fuse the vector updates (evaluated
+// at the seven stencil points) with the operator; it moves 17 FP32 vectors.
+// Dot products are formed in FP32 per thread and warp and summed across
+// warps and blocks in FP64.
 #include <algorithm>
 #include <cmath>
 
@@ -83,79 +86,160 @@ __global__ void __launch_bounds__(kBlock) k_mix_init(Mesh m, MixArgs a, RedScrat
         sc->b1 = b1; sc->b2 = b2;
         sc->iter = 0; sc->status = 0; sc->converged = 0; sc->done = 0; sc->outer = 0;
         sc->iiter = 0; sc->ksince = 0; sc->pending = 1; sc->restart = 1; sc->cur = 0;
-        sc->efresh = 1; sc->has_e = 0;
+        sc->has_e = 0; sc->einc = 0; sc->rfresh = 1;
         sc->iscale = 0.0;  // set from the first residual
-        sc->r2_upd = INFINITY;
+        sc->r2sq = 0.0; sc->rsum = 0.0; sc->theta = 1.0; sc->perturb = 0;
     }
 }
 
-// The two stencil passes process two consecutive layers of one column per
-// thread (the compact layout and an even layer count make the pair 8-byte
-// aligned), so vertical neighbours are shared and column loads are float2.
+// Both passes process two consecutive layers of one column per thread (the
+// compact layout and an even layer count make the pair 8-byte aligned), so
+// vertical neighbours are shared and column loads are float2.
 __device__ __forceinline__ float2 ld2(const float* p, size_t i) { return *reinterpret_cast<const float2*>(p + i); }
+__device__ __forceinline__ void st2(float* p, size_t i, float x, float y) {
+    *reinterpret_cast<float2*>(p + i) = make_float2(x, y);
+}
 
-// Inner pass 1: p = r + beta (p - omega v) at the stencil points,
-// v = A D^-1 p, dot (r0, v).
-__global__ void __launch_bounds__(kBlock) k_in_pv(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
-    if (sc->done || sc->pending) return;
-    const int it = sc->iiter, nz = m.NZ, NZI = m.NZI;
-    const float beta = (float)((sc->irho / sc->irho_prev) * (sc->ialpha / sc->iomega));
-    const float om = (float)sc->iomega;
+// One BiCGSTAB iteration is two passes.  The p/v pass of iteration i carries
+// the tail of iteration i-1 (r = s - omega t and the correction increment
+// e += D^-1 (alpha p + omega s)); the s/t pass forms the dots from which
+// omega, the next rho and |r|_2 follow:
+//   rho_new = (r0, s) - omega (r0, t),  |r|^2 = (s, s) - omega (t, s).
+// Inputs of the p/v pass by mode:
+//   0: first iteration of a Krylov process:  p = r
+//   1: first iteration after an FP64 update: p = r + beta (p - omega v), r stored
+//   2: otherwise:                            r = s - omega t, p = r + beta (p - omega v)
+template <int MODE>
+__device__ __forceinline__ float pv_p1(const MixArgs& a, const float* pin, const float* vin, float beta, float om,
+                                       size_t i) {
+    if (MODE == 0) return a.r[i];
+    const float r = (MODE == 1) ? a.r[i] : fmaf(-om, a.t[i], a.s[i]);
+    return fmaf(beta, fmaf(-om, vin[i], pin[i]), r);
+}
+
+template <int MODE>
+__device__ __forceinline__ float2 pv_y2(const MixArgs& a, const float* pin, const float* vin, float beta, float om,
+                                        size_t i) {  // D^-1 p at layers i, i+1
+    const float2 dd = ld2(a.invD, i);
+    float2 r;
+    if (MODE == 2) {
+        const float2 ss = ld2(a.s, i), tt = ld2(a.t, i);
+        r = make_float2(fmaf(-om, tt.x, ss.x), fmaf(-om, tt.y, ss.y));
+    } else {
+        r = ld2(a.r, i);
+    }
+    if (MODE == 0) return make_float2(r.x * dd.x, r.y * dd.y);
+    const float2 pp = ld2(pin, i), vv = ld2(vin, i);
+    return make_float2(fmaf(beta, fmaf(-om, vv.x, pp.x), r.x) * dd.x, fmaf(beta, fmaf(-om, vv.y, pp.y), r.y) * dd.y);
+}
+
+// p/v pass over the thread's pairs; f = {(r0, v), sum e, sum D^-1 p, |r|_1,
+// |r|_2^2} (the last three only in mode 2, where r is formed here).
+template <int MODE>
+__device__ __forceinline__ void pv_pairs(const Mesh& m, const MixArgs& a, int it, float beta, float om, float al,
+                                         float (&f)[5]) {
+    const int nz = m.NZ, NZI = m.NZI;
     const float* pin = (it & 1) ? a.p1 : a.p0;
     const float* vin = (it & 1) ? a.v1 : a.v0;
     float* pout = (it & 1) ? a.p0 : a.p1;
     float* vout = (it & 1) ? a.v0 : a.v1;
     const int npair = m.nprism >> 1;
-    float acc = 0.f;
-    auto pn1 = [&](size_t i) { return (it == 0) ? a.r[i] : fmaf(beta, fmaf(-om, vin[i], pin[i]), a.r[i]); };
-    auto y2 = [&](size_t i) {  // y = D^-1 p at layers i, i+1
-        const float2 rr = ld2(a.r, i), dd = ld2(a.invD, i);
-        if (it == 0) return make_float2(rr.x * dd.x, rr.y * dd.y);
-        const float2 pp = ld2(pin, i), vv = ld2(vin, i);
-        return make_float2(fmaf(beta, fmaf(-om, vv.x, pp.x), rr.x) * dd.x, fmaf(beta, fmaf(-om, vv.y, pp.y), rr.y) * dd.y);
-    };
     for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < npair; h += gridDim.x * blockDim.x) {
         const int g = 2 * h;
         const int c = g / NZI, kk = g - c * NZI;  // kk even: layers k0 = kk+1, kk+2
         const int k0 = kk + 1;
         const ColPPE32& P = a.ppe32[c];
-        const float2 rr = ld2(a.r, g), dd = ld2(a.invD, g);
-        float2 p0 = rr;
-        if (it != 0) {
-            const float2 pp = ld2(pin, g), vv = ld2(vin, g);
-            p0 = make_float2(fmaf(beta, fmaf(-om, vv.x, pp.x), rr.x), fmaf(beta, fmaf(-om, vv.y, pp.y), rr.y));
+        const float2 dd = ld2(a.invD, g);
+        float2 r, p;
+        if (MODE == 2) {
+            const float2 ss = ld2(a.s, g), tt = ld2(a.t, g), pp = ld2(pin, g), vv = ld2(vin, g);
+            r = make_float2(fmaf(-om, tt.x, ss.x), fmaf(-om, tt.y, ss.y));
+            p = make_float2(fmaf(beta, fmaf(-om, vv.x, pp.x), r.x), fmaf(beta, fmaf(-om, vv.y, pp.y), r.y));
+            // increment of the previous iteration: e += D^-1 (alpha p + omega s)
+            float2 e = ld2(a.e, g);
+            e.x = fmaf(dd.x, fmaf(om, ss.x, al * pp.x), e.x);
+            e.y = fmaf(dd.y, fmaf(om, ss.y, al * pp.y), e.y);
+            st2(a.e, g, e.x, e.y);
+            st2(a.r, g, r.x, r.y);
+            f[1] += e.x + e.y;
+            f[3] += fabsf(r.x) + fabsf(r.y);
+            f[4] = fmaf(r.x, r.x, fmaf(r.y, r.y, f[4]));
+        } else {
+            r = ld2(a.r, g);
+            p = r;
+            if (MODE == 1) {
+                const float2 pp = ld2(pin, g), vv = ld2(vin, g);
+                p = make_float2(fmaf(beta, fmaf(-om, vv.x, pp.x), r.x), fmaf(beta, fmaf(-om, vv.y, pp.y), r.y));
+            }
         }
-        const float y0a = p0.x * dd.x, y0b = p0.y * dd.y;
-        const float yB = (kk > 0) ? pn1(g - 1) * a.invD[g - 1] : 0.f;
-        const float yT = (kk + 2 < NZI) ? pn1(g + 2) * a.invD[g + 2] : 0.f;
-        const float2 n1 = y2(g + (size_t)(P.nb[0] - c) * NZI);
-        const float2 n2 = y2(g + (size_t)(P.nb[1] - c) * NZI);
-        const float2 n3 = y2(g + (size_t)(P.nb[2] - c) * NZI);
+        const float y0a = p.x * dd.x, y0b = p.y * dd.y;
+        const float yB = (kk > 0) ? pv_p1<MODE>(a, pin, vin, beta, om, g - 1) * a.invD[g - 1] : 0.f;
+        const float yT = (kk + 2 < NZI) ? pv_p1<MODE>(a, pin, vin, beta, om, g + 2) * a.invD[g + 2] : 0.f;
+        const float2 n1 = pv_y2<MODE>(a, pin, vin, beta, om, g + (size_t)(P.nb[0] - c) * NZI);
+        const float2 n2 = pv_y2<MODE>(a, pin, vin, beta, om, g + (size_t)(P.nb[1] - c) * NZI);
+        const float2 n3 = pv_y2<MODE>(a, pin, vin, beta, om, g + (size_t)(P.nb[2] - c) * NZI);
         const float va = a_row32(a, nz, P, k0, y0a, n1.x, n2.x, n3.x, y0b, yB);
         const float vb = a_row32(a, nz, P, k0 + 1, y0b, n1.y, n2.y, n3.y, yT, y0a);
-        *reinterpret_cast<float2*>(pout + g) = p0;
-        *reinterpret_cast<float2*>(vout + g) = make_float2(va, vb);
+        st2(pout, g, p.x, p.y);
+        st2(vout, g, va, vb);
         const float2 q0 = ld2(a.r0, g);
-        acc = fmaf(q0.x, va, acc);
-        acc = fmaf(q0.y, vb, acc);
+        f[0] = fmaf(q0.x, va, f[0]);
+        f[0] = fmaf(q0.y, vb, f[0]);
+        f[2] += y0a + y0b;
     }
-    double part[1] = {(double)acc}, tot[1];
-    if (grid_reduce<1, false>(part, rs, tot) && threadIdx.x == 0) {
+}
+
+// Pass 1: the previous iteration's tail, p update, v = A D^-1 p, (r0, v).
+// In mode 2 it also forms the norms of r and takes the hand-over test: when
+// it fires, alpha is left as it was, so that the pass repeated after the FP64
+// update (mode 1, same iteration index) continues the same Krylov process.
+__global__ void __launch_bounds__(kBlock) k_in_pv(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
+    if (sc->done || sc->pending) return;
+    const int it = sc->iiter;
+    const int mode = (it == 0) ? 0 : (sc->rfresh ? 1 : 2);
+    const float beta = it ? (float)((sc->irho / sc->irho_prev) * (sc->ialpha / sc->iomega)) : 0.f;
+    const float om = (float)sc->iomega, al = (float)sc->ialpha;
+    float f[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    if (mode == 2) pv_pairs<2>(m, a, it, beta, om, al, f);
+    else if (mode == 1) pv_pairs<1>(m, a, it, beta, om, al, f);
+    else pv_pairs<0>(m, a, it, beta, om, al, f);
+    double tot[5];
+    if (grid_reduce_f<5>(f, rs, tot) && threadIdx.x == 0) {
         sc->ir0v = tot[0];
+        sc->ise = tot[1];
+        sc->isy = tot[2];
+        sc->rfresh = 0;
+        sc->einc = 0;
+        if (mode == 2) {
+            const double r1 = tot[3], r2 = sqrt(tot[4]);
+            sc->ir1 = r1; sc->ir2 = r2;
+            const double rel = fmin(r1 / sc->ib1, r2 / sc->ib2);                       // since the last update
+            const double est = fmin(r1 * sc->iscale / sc->b1, r2 * sc->iscale / sc->b2);  // outer estimate
+            if (!(r2 == r2)) { sc->pending = 1; sc->restart = 1; sc->has_e = 0; }
+            else if (est < sc->eps || rel < sc->inner_tol) sc->pending = 1;
+            if (sc->pending) {
+                if (sc->iiter >= sc->restart_every) sc->restart = 1;
+                return;
+            }
+        }
         if (fabs(tot[0]) < 1.0e-30) { sc->pending = 1; sc->restart = 1; }  // breakdown: restart
         else sc->ialpha = sc->irho / tot[0];
     }
 }
 
-// Inner pass 2: s = r - alpha v at the stencil points, t = A D^-1 s,
-// dots (t, s) and (t, t).
+// Pass 2: s = r - alpha v at the stencil points, t = A D^-1 s, the dots
+// (t, s), (t, t), (r0, s), (r0, t) and sum D^-1 s; then omega, the next rho,
+// the mean of e after this iteration and the iteration-count tests.  The
+// residual tests wait for the next pass, which forms r = s - omega t
+// explicitly: |r|^2 = (s, s) - omega (t, s) cancels badly when t is nearly
+// parallel to s, as it is for smooth residuals.
 __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
     if (sc->done || sc->pending) return;
     const int it = sc->iiter, nz = m.NZ, NZI = m.NZI;
     const float al = (float)sc->ialpha;
     const float* v = (it & 1) ? a.v0 : a.v1;
     const int npair = m.nprism >> 1;
-    float ts = 0.f, tt = 0.f;
+    float f[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     auto z2 = [&](size_t i) {
         const float2 rr = ld2(a.r, i), vv = ld2(v, i), dd = ld2(a.invD, i);
         return make_float2(fmaf(-al, vv.x, rr.x) * dd.x, fmaf(-al, vv.y, rr.y) * dd.y);
@@ -176,94 +260,62 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
         const float2 n3 = z2(g + (size_t)(P.nb[2] - c) * NZI);
         const float ta = a_row32(a, nz, P, k0, z0a, n1.x, n2.x, n3.x, z0b, zB);
         const float tb = a_row32(a, nz, P, k0 + 1, z0b, n1.y, n2.y, n3.y, zT, z0a);
-        *reinterpret_cast<float2*>(a.s + g) = make_float2(s0a, s0b);
-        *reinterpret_cast<float2*>(a.t + g) = make_float2(ta, tb);
-        ts = fmaf(ta, s0a, ts); ts = fmaf(tb, s0b, ts);
-        tt = fmaf(ta, ta, tt); tt = fmaf(tb, tb, tt);
+        st2(a.s, g, s0a, s0b);
+        st2(a.t, g, ta, tb);
+        const float2 q0 = ld2(a.r0, g);
+        f[0] = fmaf(ta, s0a, f[0]); f[0] = fmaf(tb, s0b, f[0]);
+        f[1] = fmaf(ta, ta, f[1]);  f[1] = fmaf(tb, tb, f[1]);
+        f[2] = fmaf(q0.x, s0a, f[2]); f[2] = fmaf(q0.y, s0b, f[2]);
+        f[3] = fmaf(q0.x, ta, f[3]); f[3] = fmaf(q0.y, tb, f[3]);
+        f[4] += z0a + z0b;
     }
-    double part[2] = {(double)ts, (double)tt}, tot[2];
-    if (grid_reduce<2, false>(part, rs, tot) && threadIdx.x == 0) {
-        if (tot[1] > 0.0) sc->iomega = tot[0] / tot[1];
-        else { sc->pending = 1; sc->restart = 1; }
-    }
-}
-
-// Inner pass 3: e += D^-1 (alpha p + omega s), r = s - omega t, norms and
-// the next rho; inner stopping test relative to the cycle's start.
-__device__ __forceinline__ void upd_one(int fresh, float id, float al, float om, float p, float s, float t, float r0,
-                                        float& e, float& r, float& s1, float& s2, float& s3, float& s4) {
-    const float de = id * fmaf(om, s, al * p);
-    e = fresh ? de : e + de;
-    r = fmaf(-om, t, s);
-    s1 += fabsf(r);
-    s2 = fmaf(r, r, s2);
-    s3 = fmaf(r0, r, s3);
-    s4 += e;
-}
-
-__global__ void __launch_bounds__(kBlock) k_in_upd(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
-    if (sc->done || sc->pending) return;
-    const int it = sc->iiter;
-    const int fresh = sc->efresh;
-    const float al = (float)sc->ialpha, om = (float)sc->iomega;
-    const float* p = (it & 1) ? a.p0 : a.p1;
-    float s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f;
-    const int n4 = m.nprism >> 2;
-    const float4* id4 = reinterpret_cast<const float4*>(a.invD);
-    const float4* p4 = reinterpret_cast<const float4*>(p);
-    const float4* sv4 = reinterpret_cast<const float4*>(a.s);
-    const float4* t4 = reinterpret_cast<const float4*>(a.t);
-    const float4* q4 = reinterpret_cast<const float4*>(a.r0);
-    float4* e4 = reinterpret_cast<float4*>(a.e);
-    float4* r4 = reinterpret_cast<float4*>(a.r);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
-        const float4 id = id4[i], pp = p4[i], ss = sv4[i], tt = t4[i], rq = q4[i];
-        float4 ee = fresh ? make_float4(0.f, 0.f, 0.f, 0.f) : e4[i], rr;
-        upd_one(fresh, id.x, al, om, pp.x, ss.x, tt.x, rq.x, ee.x, rr.x, s1, s2, s3, s4);
-        upd_one(fresh, id.y, al, om, pp.y, ss.y, tt.y, rq.y, ee.y, rr.y, s1, s2, s3, s4);
-        upd_one(fresh, id.z, al, om, pp.z, ss.z, tt.z, rq.z, ee.z, rr.z, s1, s2, s3, s4);
-        upd_one(fresh, id.w, al, om, pp.w, ss.w, tt.w, rq.w, ee.w, rr.w, s1, s2, s3, s4);
-        e4[i] = ee;
-        r4[i] = rr;
-    }
-    for (int g = 4 * n4 + blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
-        float ee = fresh ? 0.f : a.e[g], rr;
-        upd_one(fresh, a.invD[g], al, om, p[g], a.s[g], a.t[g], a.r0[g], ee, rr, s1, s2, s3, s4);
-        a.e[g] = ee;
-        a.r[g] = rr;
-    }
-    double part[4] = {(double)s1, (double)s2, (double)s3, (double)s4}, tot[4];
-    if (grid_reduce<4, false>(part, rs, tot) && threadIdx.x == 0) {
-        const double r1 = tot[0], r2 = sqrt(tot[1]);
-        sc->ir1 = r1; sc->ir2 = r2;
-        sc->emean = tot[3] / (double)m.nprism;
+    double tot[5];
+    if (grid_reduce_f<5>(f, rs, tot) && threadIdx.x == 0) {
+        const double ts = tot[0], tt = tot[1];
+        if (!(tt > 0.0)) {  // t = 0 or not finite: restart from the FP64 truth
+            sc->pending = 1; sc->restart = 1; sc->einc = 0;
+            if (!(tt == tt)) sc->has_e = 0;
+            return;
+        }
+        const double om = ts / tt;
+        sc->iomega = om;
+        sc->emean = (sc->ise + sc->ialpha * sc->isy + om * tot[4]) / (double)m.nprism;
         sc->irho_prev = sc->irho;
-        sc->irho = tot[2];
+        sc->irho = tot[2] - om * tot[3];  // (r0, s - omega t)
         sc->iiter += 1;
         sc->ksince += 1;
         sc->iter += 1;
-        sc->efresh = 0;
         sc->has_e = 1;
-        const double rel = fmin(r1 / sc->ib1, r2 / sc->ib2);                  // since the last update
-        const double est = fmin(r1 * sc->iscale / sc->b1, r2 * sc->iscale / sc->b2);  // outer estimate
-        if (!(r2 == r2)) { sc->pending = 1; sc->restart = 1; sc->has_e = 0; }
-        else if (est < sc->eps || rel < sc->inner_tol || sc->ksince >= sc->inner_cap) sc->pending = 1;
+        sc->einc = 1;
+        if (!(om == om)) { sc->pending = 1; sc->restart = 1; sc->has_e = 0; sc->einc = 0; }
+        else if (sc->ksince >= sc->inner_cap) sc->pending = 1;
         if (sc->pending && sc->iiter >= sc->restart_every) sc->restart = 1;
         else if (sc->iter > sc->max_iters) sc->pending = 1;
-        else if (fabs(sc->irho_prev) < 1.0e-30 || fabs(sc->iomega) < 1.0e-30) { sc->pending = 1; sc->restart = 1; }
+        else if (fabs(sc->irho_prev) < 1.0e-30 || fabs(om) < 1.0e-30) { sc->pending = 1; sc->restart = 1; }
     }
 }
 
-__device__ __forceinline__ bool o_log(int k) { return k >= 0 && k < Scal::kCycLog; }
-
-// FP64 update: x <- x + iscale (e - mean e), r = b - A x, norms, the outer
-// stopping test.  Acts only when an update is pending.
+// FP64 update, first half: x1 = x + iscale (e - mean e) and r1 = b - A x1
+// into the buffers not holding the current x and r.  The correction is taken
+// whole (theta = 1, which keeps the FP32 Krylov state consistent with the
+// new residual) unless it raised |r|_2 more than 2x.  Then the FP32 process
+// went astray: the step is cut to the minimal-residual length
+//   theta = argmin |r + theta (r1 - r)|_2 = (r, r - r1) / |r - r1|^2 in [0, 1]
+// and the Krylov process restarts with a perturbed shadow residual.  (Simply
+// dropping the correction and restarting from the same residual would retrace
+// the same FP32 iterations, deterministically, forever.)
 __global__ void __launch_bounds__(kBlock) k_mix_update(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
     if (sc->done || !sc->pending) return;
     const int cur = sc->cur;
-    const double scale = sc->has_e ? sc->iscale : 0.0;
+    const int has_e = sc->has_e;
+    const int first = (sc->iscale == 0.0);
+    const int einc = has_e && sc->einc;
+    const double scale = sc->iscale;
     const float em = (float)sc->emean;
+    const float al = (float)sc->ialpha, om = (float)sc->iomega;
+    const float* pl = (sc->iiter & 1) ? a.p1 : a.p0;  // p of the last iteration
     const double* xin = cur ? a.xb : a.xa;
+    const double* rin = cur ? a.r64b : a.r64a;
     double* xout = cur ? a.xa : a.xb;
     double* rout = cur ? a.r64a : a.r64b;
     double part[3] = {0.0, 0.0, 0.0};
@@ -272,7 +324,12 @@ __global__ void __launch_bounds__(kBlock) k_mix_update(Mesh m, MixArgs a, RedScr
         prism_of(m, g, c, k0);
         const ColPPE& P = m.ppe[c];
         const size_t q = g;
-        auto xn = [&](size_t i) { return fma(scale, (double)(a.e[i] - em), xin[i]); };
+        auto xn = [&](size_t i) {
+            if (!has_e) return xin[i];
+            float e = a.e[i];
+            if (einc) e = fmaf(a.invD[i], fmaf(om, a.s[i], al * pl[i]), e);
+            return fma(scale, (double)(e - em), xin[i]);
+        };
         const double x0 = xn(q);
         const double xT = (k0 < m.NZ - 2) ? xn(q + 1) : 0.0;
         const double xB = (k0 > 1) ? xn(q - 1) : 0.0;
@@ -282,38 +339,92 @@ __global__ void __launch_bounds__(kBlock) k_mix_update(Mesh m, MixArgs a, RedScr
         xout[q] = x0;
         rout[q] = r;
         part[0] += r * r;
-        part[1] += fabs(r);
-        part[2] += r;
+        part[1] += r;
+        if (!first && has_e) part[2] += rin[q] * r;
     }
     double tot[3];
     if (grid_reduce<3, false>(part, rs, tot) && threadIdx.x == 0) {
-        const double r2 = sqrt(tot[0]), r1 = tot[1];
-        if (o_log(sc->outer)) {
-            const int k = sc->outer;
-            sc->cyc_it[k] = sc->ksince;
-            sc->cyc_in[k] = (sc->ib1 > 0.0 && sc->ksince > 0) ? (float)fmin(sc->ir1 / sc->ib1, sc->ir2 / sc->ib2) : 1.f;
-            sc->cyc_out[k] = (float)(r2 / sc->b2);
-            sc->cyc_acc[k] = sc->restart;
+        const double R1 = tot[0], C = tot[2], R0 = sc->r2sq;
+        double theta = 1.0;
+        if (!(R1 == R1)) {  // non-finite correction: drop it
+            theta = 0.0;
+            sc->restart = 1; sc->perturb = 1;
+        } else if (!first && has_e && R1 > 4.0 * R0) {
+            const double dd = R0 - 2.0 * C + R1, num = R0 - C;
+            theta = (dd > 0.0) ? num / dd : 0.0;
+            theta = fmin(fmax(theta, 0.0), 1.0);
+            sc->restart = 1; sc->perturb = 1;
         }
+        sc->theta = theta;
+        if (first) sc->iscale = (R1 > 0.0) ? sqrt(R1 / (double)m.nprism) : 1.0;
+        const double sum1 = (R1 == R1) ? tot[1] : 0.0;
+        sc->rmean = ((1.0 - theta) * sc->rsum + theta * sum1) / (double)m.nprism;
+        const int k = sc->outer % Scal::kCycLog;  // ring buffer of the last updates
+        sc->cyc_it[k] = sc->ksince;
+        sc->cyc_in[k] = (sc->ib1 > 0.0 && sc->ksince > 0 && sc->ir1 >= 0.0)
+                            ? (float)fmin(sc->ir1 / sc->ib1, sc->ir2 / sc->ib2) : 1.f;
         sc->outer += 1;
         sc->has_e = 0;
-        if (!(r2 == r2) || r2 > 2.0 * sc->r2_upd) {
-            // the FP32 process diverged: drop this correction (x and r stay in
-            // buffer `cur`) and restart the Krylov process from the truth
-            sc->restart = 1;
-            if (sc->outer >= 2000) { sc->status = NSMP_WARN_BREAKDOWN; sc->done = 1; }
-            else if (sc->iter > sc->max_iters) { sc->status = NSMP_WARN_MAXITER; sc->done = 1; }
-            return;
+        sc->einc = 0;
+    }
+}
+
+// Cheap hash in [-1, 1) of a prism index and the update count: the shadow
+// residual of a Krylov restart after a stalled cycle is perturbed by it so
+// the next cycle does not retrace the stalled one.
+__device__ __forceinline__ float shadow_jitter(unsigned int g, unsigned int k) {
+    unsigned int h = g * 2654435761u ^ (k * 40503u + 0x9e3779b9u);
+    h ^= h >> 15; h *= 0x2c1b3c6du; h ^= h >> 12; h *= 0x297a2d39u; h ^= h >> 15;
+    return (float)(h & 0xffffu) * (1.0f / 32768.0f) - 1.0f;
+}
+
+// FP64 update, second half: x, r <- x + theta (x1 - x), r + theta (r1 - r)
+// (only when theta != 1), the outer stopping test on that residual, and the
+// FP32 residual (r - mean r) / iscale with e <- 0, the norms the next update
+// is measured against and rho = (r0, r).  On a restart also r0 = r and a
+// fresh Krylov process.
+__global__ void __launch_bounds__(kBlock) k_mix_scale(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
+    if (sc->done || !sc->pending) return;
+    const int cur = sc->cur;
+    const double th = sc->theta;
+    const int blend = (th != 1.0);
+    const double inv = 1.0 / sc->iscale, rm = sc->rmean;
+    const double* xo = cur ? a.xb : a.xa;
+    const double* ro = cur ? a.r64b : a.r64a;
+    double* xn = cur ? a.xa : a.xb;
+    double* rn = cur ? a.r64a : a.r64b;
+    double part[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        double r = rn[g];
+        if (blend) {
+            r = fma(th, r - ro[g], ro[g]);
+            rn[g] = r;
+            xn[g] = fma(th, xn[g] - xo[g], xo[g]);
         }
+        part[0] += fabs(r);
+        part[1] += r * r;
+        part[2] += r;
+        const float rf = (float)((r - rm) * inv);
+        a.r[g] = rf;
+        a.e[g] = 0.f;
+        const double rd = (double)rf;
+        part[3] += fabs(rd);
+        part[4] += rd * rd;
+    }
+    double tot[5];
+    if (grid_reduce<5, false>(part, rs, tot) && threadIdx.x == 0) {
+        const double r1 = tot[0], r2 = sqrt(tot[1]);
+        const int k = (sc->outer - 1) % Scal::kCycLog;
+        sc->cyc_out[k] = (float)(r2 / sc->b2);
         sc->cur = cur ^ 1;
         sc->r1 = r1; sc->r2 = r2;
+        sc->r2sq = tot[1];
+        sc->rsum = tot[2];
         sc->e1 = r1 / sc->b1; sc->e2 = r2 / sc->b2;
-        sc->rmean = tot[2] / (double)m.nprism;
-        if (sc->iscale == 0.0) sc->iscale = (r2 > 0.0) ? r2 / sqrt((double)m.nprism) : 1.0;
-        sc->r2_upd = r2;
-        double en = 1.0e10;
-        if (en > sc->e1) en = sc->e1;
-        if (en > sc->e2) en = sc->e2;
+        sc->cyc_acc[k] = (th == 1.0 ? 1 : 0) | (sc->restart ? 2 : 0);
+        sc->ib1 = (tot[3] > 0.0) ? tot[3] : 1.0;
+        sc->ib2 = (tot[4] > 0.0) ? sqrt(tot[4]) : 1.0;
+        const double en = fmin(sc->e1, sc->e2);
         if (!(r2 == r2)) { sc->status = NSMP_ERR_NAN; sc->done = 1; }
         else if (en < sc->eps) { sc->converged = 1; sc->done = 1; }
         else if (sc->iter > sc->max_iters) { sc->status = NSMP_WARN_MAXITER; sc->done = 1; }
@@ -321,33 +432,28 @@ __global__ void __launch_bounds__(kBlock) k_mix_update(Mesh m, MixArgs a, RedScr
     }
 }
 
-// After an FP64 update: FP32 r <- (r - mean r) / iscale, recompute the norms
-// the next update is measured against and rho = (r0, r); on a restart also
-// r0 = r and a fresh Krylov process.
-__global__ void __launch_bounds__(kBlock) k_mix_scale(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
+// Shadow residual and rho for the next FP32 cycle (after k_mix_scale).
+__global__ void __launch_bounds__(kBlock) k_mix_shadow(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
     if (sc->done || !sc->pending) return;
-    const double inv = 1.0 / sc->iscale, rm = sc->rmean;
-    const int rst = sc->restart;
-    const double* r64 = sc->cur ? a.r64b : a.r64a;
-    double part[3] = {0.0, 0.0, 0.0};
+    const int rst = sc->restart, jit = sc->perturb;
+    const unsigned int salt = (unsigned int)sc->outer;
+    double part[1] = {0.0};
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
-        const float rf = (float)((r64[g] - rm) * inv);
-        a.r[g] = rf;
-        float q0 = rf;
-        if (rst) a.r0[g] = rf;
-        else q0 = a.r0[g];
-        const double rd = (double)rf;
-        part[0] += fabs(rd);
-        part[1] += rd * rd;
-        part[2] += (double)q0 * rd;
+        const float rf = a.r[g];
+        float q0;
+        if (rst) {
+            q0 = jit ? rf * (1.0f + 0.5f * shadow_jitter((unsigned int)g, salt)) : rf;
+            a.r0[g] = q0;
+        } else {
+            q0 = a.r0[g];
+        }
+        part[0] += (double)q0 * (double)rf;
     }
-    double tot[3];
-    if (grid_reduce<3, false>(part, rs, tot) && threadIdx.x == 0) {
-        sc->ib1 = (tot[0] > 0.0) ? tot[0] : 1.0;
-        sc->ib2 = (tot[1] > 0.0) ? sqrt(tot[1]) : 1.0;
-        sc->irho = tot[2];
+    double tot[1];
+    if (grid_reduce<1, false>(part, rs, tot) && threadIdx.x == 0) {
+        sc->irho = tot[0];
         if (rst) { sc->irho_prev = 1.0; sc->ialpha = 1.0; sc->iomega = 1.0; sc->iiter = 0; }
-        sc->ksince = 0; sc->pending = 0; sc->restart = 0; sc->efresh = 1;
+        sc->ksince = 0; sc->pending = 0; sc->restart = 0; sc->perturb = 0; sc->rfresh = 1; sc->einc = 0;
     }
 }
 
@@ -406,17 +512,17 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
         return NSMP_ERR_UNSUPPORTED;
     }
     const int g_pv = grid_occ(c, k_in_pv, m.nprism / 2), g_st = grid_occ(c, k_in_st, m.nprism / 2);
-    const int g_up = grid_occ(c, k_in_upd, (m.nprism + 3) / 4);
     const int g_in = grid_occ(c, k_mix_init, m.nprism), g_u = grid_occ(c, k_mix_update, m.nprism);
-    const int g_sc = grid_occ(c, k_mix_scale, m.nprism);
+    const int g_sc = grid_occ(c, k_mix_scale, m.nprism), g_sh = grid_occ(c, k_mix_shadow, m.nprism);
     MixArgs a{c->rhsp, pf, c->b64, c->r, c->x, c->xa, c->xb, c->r32, c->r032, c->p32[0], c->p32[1], c->v32[0],
               c->v32[1], c->s32, c->t32, c->e32, c->invD32, c->d_ppe32, c->lev32};
     CK(cudaMemcpyAsync(&c->d_scal->inner_tol, &c->inner_tol, sizeof(double), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(&c->d_scal->inner_cap, &c->inner_cap, sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(&c->d_scal->restart_every, &c->restart_every, sizeof(int), cudaMemcpyHostToDevice, st));
     LAUNCH(NSMP_K_BICG_INIT, k_mix_init<<<g_in, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-    LAUNCH(NSMP_K_OTHER, k_mix_update<<<g_u, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-    LAUNCH(NSMP_K_OTHER, k_mix_scale<<<g_sc, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+    LAUNCH(NSMP_K_MIX_UPDATE, k_mix_update<<<g_u, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+    LAUNCH(NSMP_K_MIX_SCALE, k_mix_scale<<<g_sc, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+    LAUNCH(NSMP_K_MIX_SCALE, k_mix_shadow<<<g_sh, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
     CKL("k_mix_init");
     // FP32 iterations in chunks, an FP64 update slot after every few
     // iterations (it only acts when one was requested); the host polls for
@@ -427,12 +533,12 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     for (;;) {
         for (int it = 0; it < chunk; it += per_update) {
             for (int j = 0; j < per_update; ++j) {
-                LAUNCH(NSMP_K_BICG_SPMV_V, k_in_pv<<<g_pv, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-                LAUNCH(NSMP_K_BICG_SPMV_T, k_in_st<<<g_st, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-                LAUNCH(NSMP_K_BICG_X, k_in_upd<<<g_up, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+                LAUNCH(NSMP_K_IN_PV, k_in_pv<<<g_pv, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+                LAUNCH(NSMP_K_IN_ST, k_in_st<<<g_st, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
             }
-            LAUNCH(NSMP_K_OTHER, k_mix_update<<<g_u, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-            LAUNCH(NSMP_K_OTHER, k_mix_scale<<<g_sc, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+            LAUNCH(NSMP_K_MIX_UPDATE, k_mix_update<<<g_u, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+            LAUNCH(NSMP_K_MIX_SCALE, k_mix_scale<<<g_sc, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+            LAUNCH(NSMP_K_MIX_SCALE, k_mix_shadow<<<g_sh, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
         }
         CKL("mixed inner chunk");
         launched += chunk;

@@ -65,9 +65,11 @@ EXPORTS = [
 ]
 
 (K_VERTEX4, K_STAGE_RHS, K_FACES_DIV, K_BICG_INIT, K_BICG_P, K_BICG_SPMV_V, K_BICG_S, K_BICG_SPMV_T,
- K_BICG_X, K_PMEAN, K_VERTEX1, K_PROJECT, K_OTHER, K_COUNT) = range(14)
+ K_BICG_X, K_PMEAN, K_VERTEX1, K_PROJECT, K_IN_PV, K_IN_ST, K_MIX_UPDATE, K_MIX_SCALE, K_OTHER,
+ K_COUNT) = range(18)
 KERNEL_NAMES = ["k_vertex4", "k_stage_rhs", "k_faces_div", "k_bicg_init", "k_bicg_p", "k_bicg_spmv_v",
-                "k_bicg_s", "k_bicg_spmv_t", "k_bicg_x", "k_pmean", "k_vertex1", "k_project", "other"]
+                "k_bicg_s", "k_bicg_spmv_t", "k_bicg_x", "k_pmean", "k_vertex1", "k_project", "k_in_pv",
+                "k_in_st", "k_mix_update", "k_mix_scale", "other"]
 
 _lib = None
 

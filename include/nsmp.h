@@ -152,35 +152,40 @@ int nsmp_set_precision(nsmp_ctx* ctx, int mode);
  * race; the first call on a device resolves the array's address and should
  * come before any stream capture. */
 int nsmp_mass_diag_noalloc(nsmp_ctx* ctx, double out[4]);
-/* NSMP_MIXED pressure solver.  The FP32 BiCGSTAB hands its correction to
- * FP64 (x += e, r = b - A x, the FP32 residual replaced by the FP64 one) when
- * its residual fell by inner_tol since the last hand-over (default 1e-1) or
- * after inner_cap iterations (default 50), and restarts its Krylov process
- * after restart_every iterations (default 300) or when a hand-over did not
- * lower the FP64 residual.  The FP64 stopping test (eps) is unaffected: these
- * trade hand-overs against iterations, not accuracy.  The mixed mode needs an
- * even number of interior layers. */
+/* NSMP_MIXED pressure solver.  The FP32 BiCGSTAB hands its correction e to
+ * FP64 when its residual fell by inner_tol since the last hand-over (default
+ * 1e-1) or after inner_cap iterations (default 50): x += e, and the FP32
+ * residual is replaced by the FP64 residual b - A x.  A correction that
+ * raised |b - A x|_2 more than 2x is cut to the step that minimises it and
+ * the Krylov process restarts with a perturbed shadow residual; it also
+ * restarts after restart_every iterations (default 300).  The FP64 stopping
+ * test (eps) is unaffected: these trade hand-overs against iterations, not
+ * accuracy.  The mixed mode needs an even number of interior layers. */
 int nsmp_set_inner_solver(nsmp_ctx* ctx, double inner_tol, int inner_cap, int restart_every);
 /* Stream used by the context (cudaStream_t as void*). */
 void* nsmp_stream(nsmp_ctx* ctx);
 
 /* ---- instrumentation ---------------------------------------------------- */
 
-/* Kernel ids for nsmp_prof_read. */
+/* Kernel ids for nsmp_prof_read.  NSMP_K_BICG_P .. NSMP_K_BICG_X are the FP64
+ * solver's passes; NSMP_K_IN_PV .. NSMP_K_MIX_SCALE the mixed solver's (FP32
+ * p/v and s/t passes, FP64 update and rescale). */
 enum {
     NSMP_K_VERTEX4 = 0, NSMP_K_STAGE_RHS, NSMP_K_FACES_DIV, NSMP_K_BICG_INIT, NSMP_K_BICG_P,
     NSMP_K_BICG_SPMV_V, NSMP_K_BICG_S, NSMP_K_BICG_SPMV_T, NSMP_K_BICG_X, NSMP_K_PMEAN,
-    NSMP_K_VERTEX1, NSMP_K_PROJECT, NSMP_K_OTHER, NSMP_K_COUNT
+    NSMP_K_VERTEX1, NSMP_K_PROJECT, NSMP_K_IN_PV, NSMP_K_IN_ST, NSMP_K_MIX_UPDATE,
+    NSMP_K_MIX_SCALE, NSMP_K_OTHER, NSMP_K_COUNT
 };
 /* on = 1 records a CUDA event pair around every kernel launch on the
  * context's stream and accumulates per-kernel device time; on = 0 stops.
  * Enabling also clears the accumulators. */
 int nsmp_prof_enable(nsmp_ctx* ctx, int on);
 int nsmp_prof_read(nsmp_ctx* ctx, int kernel_id, long long* launches, double* total_ms);
-/* NSMP_MIXED diagnostics of the last stage's pressure solve: per FP64
- * refinement cycle the FP32 inner iterations, the inner relative residual
- * reached, the FP64 relative residual after the cycle and whether the cycle
- * was accepted.  Returns the number of cycles written (at most 48). */
+/* NSMP_MIXED diagnostics of the last stage's pressure solve, for its last
+ * (at most 48) FP64 updates, oldest first: FP32 iterations since the previous
+ * update, the FP32 relative residual reached, the FP64 relative residual
+ * after the update, and flags (bit 0: correction accepted, bit 1: Krylov
+ * process restarted).  Returns the number of updates written. */
 int nsmp_solver_log(nsmp_ctx* ctx, int max_cycles, int* inner_iters, double* inner_res,
                     double* outer_res, int* accepted);
 /* Kernels launched and BiCGSTAB iterations executed since creation. */

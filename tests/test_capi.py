@@ -32,6 +32,31 @@ def test_library_exports_header():
     assert set(ng.EXPORTS) <= set(names)
 
 
+def header_enum(first):
+    """Names of the C enum whose first member is `first`, in order."""
+    src = open(os.path.join(REPO, "include", "nsmp.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    body = re.search(r"enum\s*\{([^}]*\b" + first + r"\b[^}]*)\}", src).group(1)
+    return [t.split("=")[0].strip() for t in body.split(",") if t.strip()]
+
+
+def test_kernel_ids_match_header():
+    names = header_enum("NSMP_K_VERTEX4")
+    assert names[-1] == "NSMP_K_COUNT"
+    assert ng.K_COUNT == len(names) - 1 == len(ng.KERNEL_NAMES)
+    for i, n in enumerate(names[:-1]):
+        assert getattr(ng, n[len("NSMP_"):]) == i
+        want = n[len("NSMP_K_"):].lower()
+        assert ng.KERNEL_NAMES[i].replace("k_", "", 1) == want or ng.KERNEL_NAMES[i] == want
+
+
+def test_field_ids_match_header():
+    names = header_enum("NSMP_F_U")
+    assert names[-1] == "NSMP_NFIELDS"
+    for i, n in enumerate(names[:-1]):
+        assert getattr(ng, n[len("NSMP_"):]) == i
+
+
 def test_mesh_generator_shapes_and_determinism():
     m1 = ng.make_mesh(8, 6, seed=0)
     m2 = ng.make_mesh(8, 6, seed=0)
