@@ -92,19 +92,39 @@ __global__ void __launch_bounds__(kBlock) k_mix_init(Mesh m, MixArgs a, RedScrat
     }
 }
 
-// Both passes process two consecutive layers of one column per thread (the
-// compact layout and an even layer count make the pair 8-byte aligned), so
-// vertical neighbours are shared and column loads are float2.
-__device__ __forceinline__ float2 ld2(const float* p, size_t i) { return *reinterpret_cast<const float2*>(p + i); }
-__device__ __forceinline__ void st2(float* p, size_t i, float x, float y) {
-    *reinterpret_cast<float2*>(p + i) = make_float2(x, y);
+// Both passes process L consecutive layers of one column per thread (L = 4
+// when the interior layer count allows it, else 2): the compact layout makes
+// the group 4L-byte aligned, vertical neighbours inside the group come from
+// registers, and every column load is one float4 (float2) per thread.
+template <int L>
+struct FV {
+    float v[L];
+    __device__ __forceinline__ float& operator[](int l) { return v[l]; }
+    __device__ __forceinline__ float operator[](int l) const { return v[l]; }
+};
+template <int L>
+__device__ __forceinline__ FV<L> ldv(const float* p, size_t i) {
+    FV<L> o;
+    if constexpr (L == 4) {
+        const float4 q = *reinterpret_cast<const float4*>(p + i);
+        o.v[0] = q.x; o.v[1] = q.y; o.v[2] = q.z; o.v[3] = q.w;
+    } else {
+        const float2 q = *reinterpret_cast<const float2*>(p + i);
+        o.v[0] = q.x; o.v[1] = q.y;
+    }
+    return o;
+}
+template <int L>
+__device__ __forceinline__ void stv(float* p, size_t i, const FV<L>& o) {
+    if constexpr (L == 4) *reinterpret_cast<float4*>(p + i) = make_float4(o.v[0], o.v[1], o.v[2], o.v[3]);
+    else *reinterpret_cast<float2*>(p + i) = make_float2(o.v[0], o.v[1]);
 }
 
 // One BiCGSTAB iteration is two passes.  The p/v pass of iteration i carries
 // the tail of iteration i-1 (r = s - omega t and the correction increment
-// e += D^-1 (alpha p + omega s)); the s/t pass forms the dots from which
-// omega, the next rho and |r|_2 follow:
-//   rho_new = (r0, s) - omega (r0, t),  |r|^2 = (s, s) - omega (t, s).
+// e += D^-1 (alpha p + omega s)) and forms the norms of that r; the s/t pass
+// forms the dots from which omega and the next rho follow:
+//   rho_new = (r0, s) - omega (r0, t).
 // Inputs of the p/v pass by mode:
 //   0: first iteration of a Krylov process:  p = r
 //   1: first iteration after an FP64 update: p = r + beta (p - omega v), r stored
@@ -117,75 +137,92 @@ __device__ __forceinline__ float pv_p1(const MixArgs& a, const float* pin, const
     return fmaf(beta, fmaf(-om, vin[i], pin[i]), r);
 }
 
-template <int MODE>
-__device__ __forceinline__ float2 pv_y2(const MixArgs& a, const float* pin, const float* vin, float beta, float om,
-                                        size_t i) {  // D^-1 p at layers i, i+1
-    const float2 dd = ld2(a.invD, i);
-    float2 r;
+template <int MODE, int L>
+__device__ __forceinline__ FV<L> pv_yv(const MixArgs& a, const float* pin, const float* vin, float beta, float om,
+                                       size_t i) {  // D^-1 p at layers i .. i+L-1
+    const FV<L> dd = ldv<L>(a.invD, i);
+    FV<L> r, y;
     if (MODE == 2) {
-        const float2 ss = ld2(a.s, i), tt = ld2(a.t, i);
-        r = make_float2(fmaf(-om, tt.x, ss.x), fmaf(-om, tt.y, ss.y));
+        const FV<L> ss = ldv<L>(a.s, i), tt = ldv<L>(a.t, i);
+#pragma unroll
+        for (int l = 0; l < L; ++l) r[l] = fmaf(-om, tt[l], ss[l]);
     } else {
-        r = ld2(a.r, i);
+        r = ldv<L>(a.r, i);
     }
-    if (MODE == 0) return make_float2(r.x * dd.x, r.y * dd.y);
-    const float2 pp = ld2(pin, i), vv = ld2(vin, i);
-    return make_float2(fmaf(beta, fmaf(-om, vv.x, pp.x), r.x) * dd.x, fmaf(beta, fmaf(-om, vv.y, pp.y), r.y) * dd.y);
+    if (MODE == 0) {
+#pragma unroll
+        for (int l = 0; l < L; ++l) y[l] = r[l] * dd[l];
+        return y;
+    }
+    const FV<L> pp = ldv<L>(pin, i), vv = ldv<L>(vin, i);
+#pragma unroll
+    for (int l = 0; l < L; ++l) y[l] = fmaf(beta, fmaf(-om, vv[l], pp[l]), r[l]) * dd[l];
+    return y;
 }
 
-// p/v pass over the thread's pairs; f = {(r0, v), sum e, sum D^-1 p, |r|_1,
-// |r|_2^2} (the last three only in mode 2, where r is formed here).
-template <int MODE>
-__device__ __forceinline__ void pv_pairs(const Mesh& m, const MixArgs& a, int it, float beta, float om, float al,
+// p/v pass over the thread's layer groups; f = {(r0, v), sum e, sum D^-1 p,
+// |r|_1, |r|_2^2} (e and the norms of r only in mode 2, where r is formed).
+template <int MODE, int L>
+__device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it, float beta, float om, float al,
                                          float (&f)[5]) {
     const int nz = m.NZ, NZI = m.NZI;
     const float* pin = (it & 1) ? a.p1 : a.p0;
     const float* vin = (it & 1) ? a.v1 : a.v0;
     float* pout = (it & 1) ? a.p0 : a.p1;
     float* vout = (it & 1) ? a.v0 : a.v1;
-    const int npair = m.nprism >> 1;
-    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < npair; h += gridDim.x * blockDim.x) {
-        const int g = 2 * h;
-        const int c = g / NZI, kk = g - c * NZI;  // kk even: layers k0 = kk+1, kk+2
+    const int ngrp = m.nprism / L;
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < ngrp; h += gridDim.x * blockDim.x) {
+        const int g = L * h;
+        const int c = g / NZI, kk = g - c * NZI;  // layers k0 = kk+1 .. kk+L
         const int k0 = kk + 1;
         const ColPPE32& P = a.ppe32[c];
-        const float2 dd = ld2(a.invD, g);
-        float2 r, p;
+        const FV<L> dd = ldv<L>(a.invD, g);
+        FV<L> r, p;
         if (MODE == 2) {
-            const float2 ss = ld2(a.s, g), tt = ld2(a.t, g), pp = ld2(pin, g), vv = ld2(vin, g);
-            r = make_float2(fmaf(-om, tt.x, ss.x), fmaf(-om, tt.y, ss.y));
-            p = make_float2(fmaf(beta, fmaf(-om, vv.x, pp.x), r.x), fmaf(beta, fmaf(-om, vv.y, pp.y), r.y));
-            // increment of the previous iteration: e += D^-1 (alpha p + omega s)
-            float2 e = ld2(a.e, g);
-            e.x = fmaf(dd.x, fmaf(om, ss.x, al * pp.x), e.x);
-            e.y = fmaf(dd.y, fmaf(om, ss.y, al * pp.y), e.y);
-            st2(a.e, g, e.x, e.y);
-            st2(a.r, g, r.x, r.y);
-            f[1] += e.x + e.y;
-            f[3] += fabsf(r.x) + fabsf(r.y);
-            f[4] = fmaf(r.x, r.x, fmaf(r.y, r.y, f[4]));
+            const FV<L> ss = ldv<L>(a.s, g), tt = ldv<L>(a.t, g), pp = ldv<L>(pin, g), vv = ldv<L>(vin, g);
+            FV<L> e = ldv<L>(a.e, g);
+#pragma unroll
+            for (int l = 0; l < L; ++l) {
+                r[l] = fmaf(-om, tt[l], ss[l]);
+                p[l] = fmaf(beta, fmaf(-om, vv[l], pp[l]), r[l]);
+                // increment of the previous iteration: e += D^-1 (alpha p + omega s)
+                e[l] = fmaf(dd[l], fmaf(om, ss[l], al * pp[l]), e[l]);
+                f[1] += e[l];
+                f[3] += fabsf(r[l]);
+                f[4] = fmaf(r[l], r[l], f[4]);
+            }
+            stv<L>(a.e, g, e);
+            stv<L>(a.r, g, r);
         } else {
-            r = ld2(a.r, g);
+            r = ldv<L>(a.r, g);
             p = r;
             if (MODE == 1) {
-                const float2 pp = ld2(pin, g), vv = ld2(vin, g);
-                p = make_float2(fmaf(beta, fmaf(-om, vv.x, pp.x), r.x), fmaf(beta, fmaf(-om, vv.y, pp.y), r.y));
+                const FV<L> pp = ldv<L>(pin, g), vv = ldv<L>(vin, g);
+#pragma unroll
+                for (int l = 0; l < L; ++l) p[l] = fmaf(beta, fmaf(-om, vv[l], pp[l]), r[l]);
             }
         }
-        const float y0a = p.x * dd.x, y0b = p.y * dd.y;
+        FV<L> y;
+#pragma unroll
+        for (int l = 0; l < L; ++l) y[l] = p[l] * dd[l];
         const float yB = (kk > 0) ? pv_p1<MODE>(a, pin, vin, beta, om, g - 1) * a.invD[g - 1] : 0.f;
-        const float yT = (kk + 2 < NZI) ? pv_p1<MODE>(a, pin, vin, beta, om, g + 2) * a.invD[g + 2] : 0.f;
-        const float2 n1 = pv_y2<MODE>(a, pin, vin, beta, om, g + (size_t)(P.nb[0] - c) * NZI);
-        const float2 n2 = pv_y2<MODE>(a, pin, vin, beta, om, g + (size_t)(P.nb[1] - c) * NZI);
-        const float2 n3 = pv_y2<MODE>(a, pin, vin, beta, om, g + (size_t)(P.nb[2] - c) * NZI);
-        const float va = a_row32(a, nz, P, k0, y0a, n1.x, n2.x, n3.x, y0b, yB);
-        const float vb = a_row32(a, nz, P, k0 + 1, y0b, n1.y, n2.y, n3.y, yT, y0a);
-        st2(pout, g, p.x, p.y);
-        st2(vout, g, va, vb);
-        const float2 q0 = ld2(a.r0, g);
-        f[0] = fmaf(q0.x, va, f[0]);
-        f[0] = fmaf(q0.y, vb, f[0]);
-        f[2] += y0a + y0b;
+        const float yT = (kk + L < NZI) ? pv_p1<MODE>(a, pin, vin, beta, om, g + L) * a.invD[g + L] : 0.f;
+        const FV<L> n1 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[0] - c) * NZI);
+        const FV<L> n2 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[1] - c) * NZI);
+        const FV<L> n3 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[2] - c) * NZI);
+        FV<L> v;
+#pragma unroll
+        for (int l = 0; l < L; ++l)
+            v[l] = a_row32(a, nz, P, k0 + l, y[l], n1[l], n2[l], n3[l], (l + 1 < L) ? y[l + 1] : yT,
+                           (l > 0) ? y[l - 1] : yB);
+        stv<L>(pout, g, p);
+        stv<L>(vout, g, v);
+        const FV<L> q0 = ldv<L>(a.r0, g);
+#pragma unroll
+        for (int l = 0; l < L; ++l) {
+            f[0] = fmaf(q0[l], v[l], f[0]);
+            f[2] += y[l];
+        }
     }
 }
 
@@ -193,6 +230,7 @@ __device__ __forceinline__ void pv_pairs(const Mesh& m, const MixArgs& a, int it
 // In mode 2 it also forms the norms of r and takes the hand-over test: when
 // it fires, alpha is left as it was, so that the pass repeated after the FP64
 // update (mode 1, same iteration index) continues the same Krylov process.
+template <int L>
 __global__ void __launch_bounds__(kBlock) k_in_pv(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
     if (sc->done || sc->pending) return;
     const int it = sc->iiter;
@@ -200,9 +238,9 @@ __global__ void __launch_bounds__(kBlock) k_in_pv(Mesh m, MixArgs a, RedScratch 
     const float beta = it ? (float)((sc->irho / sc->irho_prev) * (sc->ialpha / sc->iomega)) : 0.f;
     const float om = (float)sc->iomega, al = (float)sc->ialpha;
     float f[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    if (mode == 2) pv_pairs<2>(m, a, it, beta, om, al, f);
-    else if (mode == 1) pv_pairs<1>(m, a, it, beta, om, al, f);
-    else pv_pairs<0>(m, a, it, beta, om, al, f);
+    if (mode == 2) pv_cells<2, L>(m, a, it, beta, om, al, f);
+    else if (mode == 1) pv_cells<1, L>(m, a, it, beta, om, al, f);
+    else pv_cells<0, L>(m, a, it, beta, om, al, f);
     double tot[5];
     if (grid_reduce_f<5>(f, rs, tot) && threadIdx.x == 0) {
         sc->ir0v = tot[0];
@@ -233,41 +271,55 @@ __global__ void __launch_bounds__(kBlock) k_in_pv(Mesh m, MixArgs a, RedScratch 
 // residual tests wait for the next pass, which forms r = s - omega t
 // explicitly: |r|^2 = (s, s) - omega (t, s) cancels badly when t is nearly
 // parallel to s, as it is for smooth residuals.
+template <int L>
 __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
     if (sc->done || sc->pending) return;
     const int it = sc->iiter, nz = m.NZ, NZI = m.NZI;
     const float al = (float)sc->ialpha;
     const float* v = (it & 1) ? a.v0 : a.v1;
-    const int npair = m.nprism >> 1;
+    const int ngrp = m.nprism / L;
     float f[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    auto z2 = [&](size_t i) {
-        const float2 rr = ld2(a.r, i), vv = ld2(v, i), dd = ld2(a.invD, i);
-        return make_float2(fmaf(-al, vv.x, rr.x) * dd.x, fmaf(-al, vv.y, rr.y) * dd.y);
+    auto zv = [&](size_t i) {
+        const FV<L> rr = ldv<L>(a.r, i), vv = ldv<L>(v, i), dd = ldv<L>(a.invD, i);
+        FV<L> z;
+#pragma unroll
+        for (int l = 0; l < L; ++l) z[l] = fmaf(-al, vv[l], rr[l]) * dd[l];
+        return z;
     };
     auto z1 = [&](size_t i) { return fmaf(-al, v[i], a.r[i]) * a.invD[i]; };
-    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < npair; h += gridDim.x * blockDim.x) {
-        const int g = 2 * h;
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < ngrp; h += gridDim.x * blockDim.x) {
+        const int g = L * h;
         const int c = g / NZI, kk = g - c * NZI;
         const int k0 = kk + 1;
         const ColPPE32& P = a.ppe32[c];
-        const float2 rr = ld2(a.r, g), vv = ld2(v, g), dd = ld2(a.invD, g);
-        const float s0a = fmaf(-al, vv.x, rr.x), s0b = fmaf(-al, vv.y, rr.y);
-        const float z0a = s0a * dd.x, z0b = s0b * dd.y;
+        const FV<L> rr = ldv<L>(a.r, g), vv = ldv<L>(v, g), dd = ldv<L>(a.invD, g);
+        FV<L> s0, z0;
+#pragma unroll
+        for (int l = 0; l < L; ++l) {
+            s0[l] = fmaf(-al, vv[l], rr[l]);
+            z0[l] = s0[l] * dd[l];
+        }
         const float zB = (kk > 0) ? z1(g - 1) : 0.f;
-        const float zT = (kk + 2 < NZI) ? z1(g + 2) : 0.f;
-        const float2 n1 = z2(g + (size_t)(P.nb[0] - c) * NZI);
-        const float2 n2 = z2(g + (size_t)(P.nb[1] - c) * NZI);
-        const float2 n3 = z2(g + (size_t)(P.nb[2] - c) * NZI);
-        const float ta = a_row32(a, nz, P, k0, z0a, n1.x, n2.x, n3.x, z0b, zB);
-        const float tb = a_row32(a, nz, P, k0 + 1, z0b, n1.y, n2.y, n3.y, zT, z0a);
-        st2(a.s, g, s0a, s0b);
-        st2(a.t, g, ta, tb);
-        const float2 q0 = ld2(a.r0, g);
-        f[0] = fmaf(ta, s0a, f[0]); f[0] = fmaf(tb, s0b, f[0]);
-        f[1] = fmaf(ta, ta, f[1]);  f[1] = fmaf(tb, tb, f[1]);
-        f[2] = fmaf(q0.x, s0a, f[2]); f[2] = fmaf(q0.y, s0b, f[2]);
-        f[3] = fmaf(q0.x, ta, f[3]); f[3] = fmaf(q0.y, tb, f[3]);
-        f[4] += z0a + z0b;
+        const float zT = (kk + L < NZI) ? z1(g + L) : 0.f;
+        const FV<L> n1 = zv(g + (size_t)(P.nb[0] - c) * NZI);
+        const FV<L> n2 = zv(g + (size_t)(P.nb[1] - c) * NZI);
+        const FV<L> n3 = zv(g + (size_t)(P.nb[2] - c) * NZI);
+        FV<L> t;
+#pragma unroll
+        for (int l = 0; l < L; ++l)
+            t[l] = a_row32(a, nz, P, k0 + l, z0[l], n1[l], n2[l], n3[l], (l + 1 < L) ? z0[l + 1] : zT,
+                           (l > 0) ? z0[l - 1] : zB);
+        stv<L>(a.s, g, s0);
+        stv<L>(a.t, g, t);
+        const FV<L> q0 = ldv<L>(a.r0, g);
+#pragma unroll
+        for (int l = 0; l < L; ++l) {
+            f[0] = fmaf(t[l], s0[l], f[0]);
+            f[1] = fmaf(t[l], t[l], f[1]);
+            f[2] = fmaf(q0[l], s0[l], f[2]);
+            f[3] = fmaf(q0[l], t[l], f[3]);
+            f[4] += z0[l];
+        }
     }
     double tot[5];
     if (grid_reduce_f<5>(f, rs, tot) && threadIdx.x == 0) {
@@ -511,7 +563,11 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
         c->err = "mixed precision needs an even number of layers";
         return NSMP_ERR_UNSUPPORTED;
     }
-    const int g_pv = grid_occ(c, k_in_pv, m.nprism / 2), g_st = grid_occ(c, k_in_st, m.nprism / 2);
+    // four layers per thread when the interior layer count allows it
+    const bool quad = (m.NZI % 4) == 0;
+    const int L = quad ? 4 : 2;
+    const int g_pv = quad ? grid_occ(c, k_in_pv<4>, m.nprism / L) : grid_occ(c, k_in_pv<2>, m.nprism / L);
+    const int g_st = quad ? grid_occ(c, k_in_st<4>, m.nprism / L) : grid_occ(c, k_in_st<2>, m.nprism / L);
     const int g_in = grid_occ(c, k_mix_init, m.nprism), g_u = grid_occ(c, k_mix_update, m.nprism);
     const int g_sc = grid_occ(c, k_mix_scale, m.nprism), g_sh = grid_occ(c, k_mix_shadow, m.nprism);
     MixArgs a{c->rhsp, pf, c->b64, c->r, c->x, c->xa, c->xb, c->r32, c->r032, c->p32[0], c->p32[1], c->v32[0],
@@ -533,8 +589,13 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     for (;;) {
         for (int it = 0; it < chunk; it += per_update) {
             for (int j = 0; j < per_update; ++j) {
-                LAUNCH(NSMP_K_IN_PV, k_in_pv<<<g_pv, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-                LAUNCH(NSMP_K_IN_ST, k_in_st<<<g_st, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+                if (quad) {
+                    LAUNCH(NSMP_K_IN_PV, k_in_pv<4><<<g_pv, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+                    LAUNCH(NSMP_K_IN_ST, k_in_st<4><<<g_st, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+                } else {
+                    LAUNCH(NSMP_K_IN_PV, k_in_pv<2><<<g_pv, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+                    LAUNCH(NSMP_K_IN_ST, k_in_st<2><<<g_st, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+                }
             }
             LAUNCH(NSMP_K_MIX_UPDATE, k_mix_update<<<g_u, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
             LAUNCH(NSMP_K_MIX_SCALE, k_mix_scale<<<g_sc, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
