@@ -171,14 +171,19 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
     float* pout = (it & 1) ? a.p0 : a.p1;
     float* vout = (it & 1) ? a.v0 : a.v1;
     const int ngrp = m.nprism / L;
-    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < ngrp; h += gridDim.x * blockDim.x) {
-        const int g = L * h;
+    const int lane = threadIdx.x & 31;
+    // warp-uniform trip count: the vertical neighbours of a group are the
+    // end layers of the adjacent lanes' groups (shuffled, not reloaded)
+    for (int hw = blockIdx.x * blockDim.x + (threadIdx.x & ~31); hw < ngrp; hw += gridDim.x * blockDim.x) {
+        const int h = hw + lane;
+        const bool act = h < ngrp;
+        const int g = L * (act ? h : hw);
         const int c = g / NZI, kk = g - c * NZI;  // layers k0 = kk+1 .. kk+L
         const int k0 = kk + 1;
         const ColPPE32& P = a.ppe32[c];
         const FV<L> dd = ldv<L>(a.invD, g);
         FV<L> r, p;
-        if (MODE == 2) {
+        if (MODE == 2 && act) {
             const FV<L> ss = ldv<L>(a.s, g), tt = ldv<L>(a.t, g), pp = ldv<L>(pin, g), vv = ldv<L>(vin, g);
             FV<L> e = ldv<L>(a.e, g);
 #pragma unroll
@@ -193,6 +198,9 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
             }
             stv<L>(a.e, g, e);
             stv<L>(a.r, g, r);
+        } else if (MODE == 2) {
+#pragma unroll
+            for (int l = 0; l < L; ++l) { r[l] = 0.f; p[l] = 0.f; }
         } else {
             r = ldv<L>(a.r, g);
             p = r;
@@ -205,8 +213,13 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
         FV<L> y;
 #pragma unroll
         for (int l = 0; l < L; ++l) y[l] = p[l] * dd[l];
-        const float yB = (kk > 0) ? pv_p1<MODE>(a, pin, vin, beta, om, g - 1) * a.invD[g - 1] : 0.f;
-        const float yT = (kk + L < NZI) ? pv_p1<MODE>(a, pin, vin, beta, om, g + L) * a.invD[g + L] : 0.f;
+        float yT = __shfl_down_sync(0xffffffffu, y[0], 1);
+        float yB = __shfl_up_sync(0xffffffffu, y[L - 1], 1);
+        if (!act) continue;
+        if (kk + L >= NZI) yT = 0.f;
+        else if (lane == 31 || h + 1 >= ngrp) yT = pv_p1<MODE>(a, pin, vin, beta, om, g + L) * a.invD[g + L];
+        if (kk == 0) yB = 0.f;
+        else if (lane == 0) yB = pv_p1<MODE>(a, pin, vin, beta, om, g - 1) * a.invD[g - 1];
         const FV<L> n1 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[0] - c) * NZI);
         const FV<L> n2 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[1] - c) * NZI);
         const FV<L> n3 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[2] - c) * NZI);
@@ -287,8 +300,11 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
         return z;
     };
     auto z1 = [&](size_t i) { return fmaf(-al, v[i], a.r[i]) * a.invD[i]; };
-    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < ngrp; h += gridDim.x * blockDim.x) {
-        const int g = L * h;
+    const int lane = threadIdx.x & 31;
+    for (int hw = blockIdx.x * blockDim.x + (threadIdx.x & ~31); hw < ngrp; hw += gridDim.x * blockDim.x) {
+        const int h = hw + lane;
+        const bool act = h < ngrp;
+        const int g = L * (act ? h : hw);
         const int c = g / NZI, kk = g - c * NZI;
         const int k0 = kk + 1;
         const ColPPE32& P = a.ppe32[c];
@@ -299,8 +315,13 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
             s0[l] = fmaf(-al, vv[l], rr[l]);
             z0[l] = s0[l] * dd[l];
         }
-        const float zB = (kk > 0) ? z1(g - 1) : 0.f;
-        const float zT = (kk + L < NZI) ? z1(g + L) : 0.f;
+        float zT = __shfl_down_sync(0xffffffffu, z0[0], 1);
+        float zB = __shfl_up_sync(0xffffffffu, z0[L - 1], 1);
+        if (!act) continue;
+        if (kk + L >= NZI) zT = 0.f;
+        else if (lane == 31 || h + 1 >= ngrp) zT = z1(g + L);
+        if (kk == 0) zB = 0.f;
+        else if (lane == 0) zB = z1(g - 1);
         const FV<L> n1 = zv(g + (size_t)(P.nb[0] - c) * NZI);
         const FV<L> n2 = zv(g + (size_t)(P.nb[1] - c) * NZI);
         const FV<L> n3 = zv(g + (size_t)(P.nb[2] - c) * NZI);
