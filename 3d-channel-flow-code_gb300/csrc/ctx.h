@@ -49,6 +49,8 @@ struct nsmp_ctx {
     int restart_every = 300;      // most FP32 iterations of one Krylov process
     int last_outer = 0;
     double* stage_buf = nullptr;  // (N_CELL,NZ) staging for transfers
+    double* fx = nullptr;         // body force on u (cell layout), null when unset
+    struct AdjScratch* adj = nullptr;  // discrete-adjoint work buffers (lazily allocated)
     // reductions and scalars
     nsmp::RedScratch red{}, red2{};
     nsmp::Scal* d_scal = nullptr;
@@ -92,6 +94,11 @@ int run_pressure_fp64(nsmp_ctx* c, const double* pf, const double** x_final);
 // Pressure solve of one stage in mixed precision; on return *x_final points
 // at the FP64 solution (before the Glob_Norm mean removal).
 int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final);
+int run_adjoint(nsmp_ctx* c, int nsteps, int ckpt_every, const double* fx, double* grad, double* J);
+int run_apply_A(nsmp_ctx* c, int transpose, const double* x, double* y);
+int run_set_body_force(nsmp_ctx* c, const double* fx);
+int run_wall_shear(nsmp_ctx* c, double* tau);
+void adj_free(nsmp_ctx* c);
 int prof_begin(nsmp_ctx* c, int kid);   // returns event slot or -1
 void prof_end(nsmp_ctx* c, int slot);
 int prof_resolve(nsmp_ctx* c);

@@ -23,6 +23,7 @@ struct Scal {
     double rho, rho_prev, alpha, omega, r0v, ts, tt;
     double b1, b2, r1, r2, e1, e2;
     double diag[4];
+    double jval, jsum;     // wall-shear objective, adjoint mean-removal sum
     int iter, done, converged, status;
     int max_iters, pad;
     double eps;

@@ -61,6 +61,7 @@ struct StageArgs {
     double *hu, *hv, *hw;               // AB2 history in/out
     double *us, *vs, *ws;               // predictor out
     double* eddy;
+    const double* fx;                   // body force on u per cell, or null
     double c1, c2, dt, inv_re, bdx, bdy, bdz;
     int les, les_van;
 };
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(kBlock) k_stage_rhs(Mesh m, StageArgs a, RedSc
         const double av = Vf[0] * F1 + Vf[1] * F2 + Vf[2] * F3 + VT * FT + VB * FB;
         const double aw = Wf[0] * F1 + Wf[1] * F2 + Wf[2] * F3 + WT * FT + WB * FB;
         const double ivol = G.inv_area * lev(m, LV_IDSV, k0);
-        const double ru = a.bdx + gam * su * ivol - au * ivol;
+        const double ru = (a.fx ? a.bdx + a.fx[q] : a.bdx) + gam * su * ivol - au * ivol;
         const double rv = a.bdy + gam * sv * ivol - av * ivol;
         const double rw = a.bdz + gam * sw * ivol - aw * ivol;
         // predictor (hydro.F90:322-333)
@@ -514,6 +515,7 @@ int run_stage(nsmp_ctx* c, int fin_rk, nsmp_stage_info* info) {
     sa.c2 = (c->flag_ab == 1) ? -0.55 : 0.0;
     sa.dt = P.dt; sa.inv_re = 1.0 / P.re; sa.bdx = P.bdx; sa.bdy = P.bdy; sa.bdz = P.bdz;
     sa.les = P.les; sa.les_van = P.les_van;
+    sa.fx = c->fx;
     LAUNCH(NSMP_K_STAGE_RHS, k_stage_rhs<<<grid_occ(c, k_stage_rhs, m.nprism), kBlock, 0, st>>>(m, sa, c->red, c->d_scal));
     CKL("k_stage_rhs");
     FaceArgs fa{c->ustar[0], c->ustar[1], c->ustar[2], c->vtx[3], c->face[0], c->face[1], c->face[2],
@@ -699,6 +701,7 @@ int ctx_init_device(nsmp_ctx* c) {
 
 void ctx_free(nsmp_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
+    adj_free(c);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     c->ev_pool.clear();
     for (void* p : c->allocs) cudaFree(p);

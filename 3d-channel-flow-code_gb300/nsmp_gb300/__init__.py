@@ -62,6 +62,7 @@ EXPORTS = [
     "nsmp_set_precision", "nsmp_stream", "nsmp_mesh_size", "nsmp_mesh_generate", "nsmp_initial_channel",
     "nsmp_sigma_grid", "nsmp_geometry", "nsmp_prof_enable", "nsmp_prof_read", "nsmp_counters",
     "nsmp_set_inner_solver", "nsmp_solver_log", "nsmp_mass_diag_noalloc",
+    "nsmp_set_body_force", "nsmp_wall_shear", "nsmp_adjoint", "nsmp_apply_A", "nsmp_apply_AT",
 ]
 
 (K_VERTEX4, K_STAGE_RHS, K_FACES_DIV, K_BICG_INIT, K_BICG_P, K_BICG_SPMV_V, K_BICG_S, K_BICG_SPMV_T,
@@ -108,6 +109,11 @@ def lib(build_if_missing=True):
     L.nsmp_mass_diag_noalloc.argtypes = [vp, vp]
     L.nsmp_set_precision.argtypes = [vp, C.c_int]
     L.nsmp_set_inner_solver.argtypes = [vp, C.c_double, C.c_int, C.c_int]
+    L.nsmp_set_body_force.argtypes = [vp, vp]
+    L.nsmp_wall_shear.argtypes = [vp, P(C.c_double)]
+    L.nsmp_adjoint.argtypes = [vp, C.c_int, C.c_int, vp, vp, P(C.c_double)]
+    L.nsmp_apply_A.argtypes = [vp, vp, vp]
+    L.nsmp_apply_AT.argtypes = [vp, vp, vp]
     L.nsmp_stream.argtypes = [vp]
     L.nsmp_stream.restype = vp
     L.nsmp_mesh_size.argtypes = [C.c_int, C.c_int, P(C.c_int), P(C.c_int)]
@@ -293,6 +299,42 @@ class Solver:
         out = np.zeros(4, dtype=np.float64)
         self._check(self.L.nsmp_mass_diag(self.h, _p(out)))
         return out
+
+    # ---- discrete adjoint ------------------------------------------------
+    def _n0nz(self, a):
+        a = np.asfortranarray(np.asarray(a, dtype=np.float64))
+        if a.shape != (self.n0, self.nz):
+            raise ValueError(f"expected shape {(self.n0, self.nz)}, got {a.shape}")
+        return a
+
+    def set_body_force(self, fx):
+        """Body force on u per cell, (N0, NZ); None removes it."""
+        if fx is None:
+            self._check(self.L.nsmp_set_body_force(self.h, None))
+            return
+        fx = self._n0nz(fx)
+        self._check(self.L.nsmp_set_body_force(self.h, _p(fx)))
+
+    def wall_shear(self):
+        t = C.c_double()
+        self._check(self.L.nsmp_wall_shear(self.h, C.byref(t)))
+        return t.value
+
+    def adjoint(self, nsteps, ckpt_every, fx):
+        """(J, dJ/dfx, status): nsteps RK3 steps with body force fx and the
+        discrete adjoint of the time-averaged wall shear stress."""
+        fx = self._n0nz(fx)
+        grad = np.zeros_like(fx, order="F")
+        J = C.c_double()
+        rc = self._check(self.L.nsmp_adjoint(self.h, int(nsteps), int(ckpt_every), _p(fx), _p(grad), C.byref(J)))
+        return J.value, grad, rc
+
+    def apply_A(self, x, transpose=False):
+        x = self._n0nz(x)
+        y = np.zeros_like(x, order="F")
+        fn = self.L.nsmp_apply_AT if transpose else self.L.nsmp_apply_A
+        self._check(fn(self.h, _p(x), _p(y)))
+        return y
 
     def mass_diag_noalloc(self):
         """nsmp_mass_diag_noalloc: the same reductions with no allocation."""

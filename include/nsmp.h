@@ -165,6 +165,32 @@ int nsmp_set_inner_solver(nsmp_ctx* ctx, double inner_tol, int inner_cap, int re
 /* Stream used by the context (cudaStream_t as void*). */
 void* nsmp_stream(nsmp_ctx* ctx);
 
+/* ---- discrete adjoint (an extension: the reference has none) ------------ */
+
+/* Body force on u per cell, (N0,NZ) column-major in the original cell
+ * numbering (the ghost layers k = 1 and NZ are ignored), added to the u
+ * right-hand side of every stage next to bdx (hydro.F90:322-333).  NULL
+ * removes it. */
+int nsmp_set_body_force(nsmp_ctx* ctx, const double* fx);
+/* Wall shear stress of level n averaged over both walls:
+ * sum_c area_c nu (u(c,2)/h_2 + u(c,NZ-1)/h_NZ-1) / (2 sum_c area_c), with
+ * h the half height of the layer next to the wall and nu = 1/re. */
+int nsmp_wall_shear(nsmp_ctx* ctx, double* tau);
+/* From the current state: nsteps SSP-RK3 steps with body force fx (as
+ * nsmp_set_body_force), J = mean over steps 1..nsteps of nsmp_wall_shear,
+ * and the gradient dJ/dfx, (N0,NZ) like fx, by the discrete adjoint of the
+ * steps.  The state is checkpointed every ckpt_every steps and each segment
+ * is recomputed once during the reverse sweep (device memory: 9 cell fields
+ * per checkpoint plus 24 per step of one segment).  The context ends at the
+ * state after the nsteps steps with fx still set.  Returns the worst status
+ * of the forward and adjoint pressure solves. */
+int nsmp_adjoint(nsmp_ctx* ctx, int nsteps, int ckpt_every, const double* fx,
+                 double* grad_out, double* J_out);
+/* y = A x and y = A^T x for the PPE operator (PDE.F90:69-121) on interior
+ * fields (N0,NZ): the hooks of the dot-product test <A v, w> = <v, A^T w>. */
+int nsmp_apply_A(nsmp_ctx* ctx, const double* x, double* y);
+int nsmp_apply_AT(nsmp_ctx* ctx, const double* x, double* y);
+
 /* ---- instrumentation ---------------------------------------------------- */
 
 /* Kernel ids for nsmp_prof_read.  NSMP_K_BICG_P .. NSMP_K_BICG_X are the FP64

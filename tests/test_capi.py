@@ -19,7 +19,7 @@ def header_functions():
             continue
         src = open(os.path.join(REPO, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-        names += re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_\s\*]*?\b(nsmp_[a-z0-9_]+)\s*\(", src, flags=re.M)
+        names += re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_\s\*]*?\b(nsmp_[A-Za-z0-9_]+)\s*\(", src, flags=re.M)
     return sorted(set(names))
 
 
