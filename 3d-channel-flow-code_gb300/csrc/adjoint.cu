@@ -639,6 +639,14 @@ int adj_stage(nsmp_ctx* c, const double* in, double* const* Aout, double* const*
     const double* lam = nullptr;
     int rc = run_pressure_fp64(c, S.zero, &lam);
     if (rc < 0) return rc;
+    CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    c->bicg_iters += c->h_scal->iter;
+    if (c->h_scal->status < 0) {
+        c->err = "adjoint pressure solve: non-finite residual";
+        return c->h_scal->status;
+    }
+    rc = std::max(rc, c->h_scal->status);
     LAUNCH(NSMP_K_OTHER, k_adj_sum<<<gp, kBlock, 0, st>>>(m, lam, c->red, c->d_scal));
     LAUNCH(NSMP_K_OTHER, k_adj_center<<<gp, kBlock, 0, st>>>(m, lam, S.arhs, c->d_scal));
     // face pass

@@ -415,6 +415,99 @@ def run_ours(args):
     return 0
 
 
+def run_accuracy(args):
+    """Mixed vs FP64 after N RK3 steps from the same initial state: relative
+    L2 of u, v, w, p over the interior and the max |div| of each run."""
+    import nsmp_gb300 as ng
+
+    nx, ny, layers, dt = WORKLOADS[args.workload]
+    mesh = ng.make_mesh(nx, ny)
+    sol = {}
+    for prec in ("fp64", "mixed"):
+        prm = ng.channel_params(nx, ny, layers, dt, precision=(ng.MIXED if prec == "mixed" else ng.FP64))
+        s = ng.Solver(prm, mesh)
+        u0, v0, w0, p0 = ng.initial_channel(prm, s.ncell, seed=1)
+        s.user_initial(u0, v0, w0, p0)
+        worst = 0
+        t0 = time.perf_counter()
+        for _ in range(args.accuracy_steps):
+            rc, _ = s.step(3, 1)
+            worst = max(worst, rc)
+        sol[prec] = {"fields": {nm: s.download(f)[:prm["n0"], 1:-1] for nm, f in
+                                (("u", ng.F_U), ("v", ng.F_V), ("w", ng.F_W), ("p", ng.F_P))},
+                     "div": s.mass_diag(), "status": worst, "s": time.perf_counter() - t0}
+        s.close()
+    a, b = sol["mixed"], sol["fp64"]
+    out = {"accuracy": "mixed vs fp64", "workload": workload_desc(args.workload), "steps": args.accuracy_steps}
+    for nm in ("u", "v", "w", "p"):
+        out[f"rel_l2_{nm}"] = float(np.linalg.norm(a["fields"][nm] - b["fields"][nm]) / np.linalg.norm(b["fields"][nm]))
+    out["max_div_mixed"], out["max_div_fp64"] = float(a["div"][1]), float(b["div"][1])
+    out["max_div_diff"] = abs(out["max_div_mixed"] - out["max_div_fp64"])
+    out["status"] = {"mixed": a["status"], "fp64": b["status"]}
+    out["wall_s"] = {"mixed": round(a["s"], 1), "fp64": round(b["s"], 1)}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_adjoint_bench(args):
+    """Adjoint/forward cost: N FP64 RK3 steps forward, then the same N steps
+    through nsmp_adjoint (forward sweep with checkpoints every K steps,
+    segment recomputation and the reverse sweep) with a seeded body force."""
+    import torch
+
+    import nsmp_gb300 as ng
+
+    nx, ny, layers, dt = WORKLOADS[args.workload]
+    prisms = 2 * nx * ny * layers
+    mesh = ng.make_mesh(nx, ny)
+    prm = ng.channel_params(nx, ny, layers, dt, precision=ng.FP64)
+    s = ng.Solver(prm, mesh)
+    u0, v0, w0, p0 = ng.initial_channel(prm, s.ncell, seed=1)
+    s.user_initial(u0, v0, w0, p0)
+    n0, nz = prm["n0"], prm["nz"]
+    fx = np.zeros((n0, nz), order="F")
+    fx[:, 1:-1] = 0.01 * np.random.default_rng(2).standard_normal((n0, nz - 2))
+    cells = [s.download(f) for f in (ng.F_U, ng.F_V, ng.F_W, ng.F_P)]
+    faces = [s.download(f) for f in (ng.F_U1FACE, ng.F_U2FACE, ng.F_U3FACE, ng.F_UTFACE, ng.F_UBFACE)]
+    hist = [s.download(f) for f in (ng.F_RHSU, ng.F_RHSV, ng.F_RHSW)]
+    stream = torch.cuda.ExternalStream(s.stream)
+    N, K = args.adjoint_steps, args.ckpt
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3, out
+
+    s.set_body_force(fx)
+    s.upload_state(*cells, faces, hist, 0)
+    s.step(3, 1)  # warm-up (first-use allocations, occupancy queries)
+    s.upload_state(*cells, faces, hist, 0)
+    l0, i0 = s.counters()
+    t_fwd, _ = timed(lambda: [s.step(3, 1) for _ in range(N)])
+    l1, i1 = s.counters()
+    s.upload_state(*cells, faces, hist, 0)
+    t_adj, (J, grad, rc) = timed(lambda: s.adjoint(N, K, fx))
+    l2, i2 = s.counters()
+    ncf = n0 * nz
+    nseg = -(-N // K)
+    dev_bytes = 8 * ncf * (30 + 9 * (nseg + 1) + 24 * K)
+    line = {"metric": "adjoint/forward time", "value": t_adj / t_fwd, "unit": "x", "higher_is_better": False,
+            "workload": workload_desc(args.workload), "prisms": prisms, "steps": N, "ckpt_every": K,
+            "forward_s": t_fwd, "adjoint_s": t_adj, "J": J, "grad_l2": float(np.linalg.norm(grad)),
+            "status": rc, "bicgstab_iters_forward": i1 - i0, "bicgstab_iters_adjoint_call": i2 - i1,
+            "adjoint_device_bytes": dev_bytes,
+            "adjoint_device_bytes_note": "work buffers of nsmp_adjoint (30 cell fields + 9 per checkpoint + 24 per "
+                                         "step of one segment), on top of the context's forward state",
+            "gpu_launches": l2 - l1, "dtype": "f64"}
+    print(json.dumps(line), flush=True)
+    s.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -426,7 +519,16 @@ def main():
     ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"])
     ap.add_argument("--profile-run", action="store_true",
                     help="device-timed region only (no end-to-end leg, no CPU baseline), for ncu captures")
+    ap.add_argument("--accuracy-steps", type=int, default=0,
+                    help="instead of timing: run both precisions N RK3 steps and print mixed-vs-FP64 errors")
+    ap.add_argument("--adjoint-steps", type=int, default=0,
+                    help="instead of timing the forward: adjoint/forward cost over N FP64 RK3 steps")
+    ap.add_argument("--ckpt", type=int, default=20, help="checkpoint spacing of --adjoint-steps")
     args = ap.parse_args()
+    if args.accuracy_steps > 0:
+        return run_accuracy(args)
+    if args.adjoint_steps > 0:
+        return run_adjoint_bench(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
