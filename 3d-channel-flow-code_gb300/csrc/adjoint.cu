@@ -17,9 +17,11 @@
 // to neighbour cells and vertex classes are accumulated with FP64 atomics,
 // so the last bits of the gradient depend on the order in which blocks run.
 //
-// Memory: checkpoints of the state every `ckpt_every` steps; during the
-// reverse sweep one segment is recomputed and the inputs of each of its
-// stages (u, v, w with ghost layers and the five face fluxes) are kept.
+// Memory: checkpoints of the state every `ckpt_every` steps and the PPE
+// solution of every stage (the pressure tape); during the reverse sweep one
+// segment is recomputed from its checkpoint, replaying the taped pressures
+// instead of solving again, and the inputs of each of its stages (u, v, w
+// with ghost layers and the five face fluxes) are kept.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -37,7 +39,9 @@ struct AdjScratch {
     double* avx[4] = {};    // adjoint of the vertex fields (class layout)
     double* vtx[3] = {};    // recomputed vertex values of the stage input
     double* afx = nullptr;  // gradient accumulator (cell layout)
-    double* zero = nullptr; // zero cell field: initial guess of the adjoint solve
+    double* zero = nullptr; // zero cell field
+    double* lamc = nullptr; // last adjoint pressure solution (cell layout, unscaled)
+    double* guess = nullptr;// initial guess of the next adjoint solve (cell layout)
     double* fx_host_stage = nullptr;
     int* tptr = nullptr;    // transposed vertex stencil: cell -> (class, weight)
     int* tcls = nullptr;
@@ -209,24 +213,65 @@ __global__ void __launch_bounds__(kBlock) k_adj_sum(Mesh m, const double* __rest
 }
 
 // rhs = P2^T p_bar with its plain mean removed: p_bar - h S / H - (S - S hsum / H) / N,
-// S = sum p_bar, h = area * hmean weight, hsum = sum h (so the result sums to 0).
-__global__ void k_adj_solve_rhs(Mesh m, const double* __restrict__ pb, double* __restrict__ rhs, double hsum,
-                                Scal* sc) {
+// S = sum p_bar, h = area * hmean weight, hsum = sum h (so the result sums to 0),
+// and |rhs|_2.
+__global__ void __launch_bounds__(kBlock) k_adj_solve_rhs(Mesh m, const double* __restrict__ pb,
+                                                          double* __restrict__ rhs, double hsum, RedScratch rs,
+                                                          Scal* sc) {
     const double S = sc->jsum, H = m.tv_lsig;
     const double cst = (S - S * hsum / H) / (double)m.nprism;
+    double part[1] = {0.0};
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
         int c, k0;
         prism_of(m, g, c, k0);
-        rhs[g] = pb[g] - m.ppe[c].area * lev(m, LV_HMEAN, k0) * S / H - cst;
+        const double y = pb[g] - m.ppe[c].area * lev(m, LV_HMEAN, k0) * S / H - cst;
+        rhs[g] = y;
+        part[0] += y * y;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) sc->sum_rhs = 0.0;
+    double tot[1];
+    if (grid_reduce<1, false>(part, rs, tot) && threadIdx.x == 0) {
+        sc->adjn = sqrt(tot[0]);
+        sc->sum_rhs = 0.0;
+    }
 }
 
-// rhs_bar = lambda - mean(lambda)
+// The solve sees the right-hand side scaled to unit norm: the adjoint
+// values are small, and BiCGSTAB's breakdown tests are absolute
+// (bicgstab.F90:479-517).
+__global__ void k_adj_unit(Mesh m, double* __restrict__ rhs, const Scal* sc) {
+    const double n = sc->adjn;
+    const double inv = (n > 0.0) ? 1.0 / n : 1.0;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) rhs[g] *= inv;
+}
+
+// The adjoint pressure varies slowly from stage to stage, as the forward
+// pressure does: the last solution, scaled to the new right-hand side's norm,
+// starts the next solve.
+__global__ void k_adj_guess(Mesh m, const double* __restrict__ lamc, double* __restrict__ guess, const Scal* sc) {
+    const double n = sc->adjn;
+    const double inv = (n > 0.0) ? 1.0 / n : 0.0;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const size_t q = cell_of(g, c);
+        guess[q] = lamc[q] * inv;
+    }
+}
+
+__global__ void k_adj_keep(Mesh m, const double* __restrict__ lam, double* __restrict__ lamc, const Scal* sc) {
+    const double n = sc->adjn;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        lamc[cell_of(g, c)] = lam[g] * n;
+    }
+}
+
+// rhs_bar = (lambda - mean(lambda)) * |rhs|_2
 __global__ void k_adj_center(Mesh m, const double* __restrict__ lam, double* __restrict__ out, const Scal* sc) {
-    const double mean = sc->jsum / (double)m.nprism;
+    const double mean = sc->jsum / (double)m.nprism, n = sc->adjn;
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x)
-        out[g] = lam[g] - mean;
+        out[g] = (lam[g] - mean) * n;
 }
 
 // ---------------------------------------------------------------------------
@@ -512,6 +557,8 @@ int adj_alloc(nsmp_ctx* c) {
     CK(dalloc((void**)&S.arhs, ncmp * sizeof(double)));
     CK(dalloc((void**)&S.afx, ncf * sizeof(double)));
     CK(dalloc((void**)&S.zero, ncf * sizeof(double)));
+    CK(dalloc((void**)&S.lamc, ncf * sizeof(double)));
+    CK(dalloc((void**)&S.guess, ncf * sizeof(double)));
     // transposed vertex stencil (cell -> classes), deterministic order
     std::vector<std::vector<std::pair<int, double>>> rows(L.N0);
     for (int v = 0; v < L.nclass; ++v)
@@ -575,8 +622,10 @@ int copy_state(nsmp_ctx* c, double* buf, bool save) {
 
 // One SSP-RK3 step (as nsmp_step composes it); when `keep` is set the input
 // of stage s (u, v, w of the known level with ghosts, then the 5 face
-// fluxes) is copied to keep + s * 8 * ncf before the stage runs.
-int rk3_step(nsmp_ctx* c, double* keep, int* worst) {
+// fluxes) is copied to keep + s * 8 * ncf before the stage runs.  With
+// `tape` the stage's PPE solution is recorded at tape + s * nprism; with
+// `replay` it is taken from there instead of solving.
+int rk3_step(nsmp_ctx* c, double* keep, double* tape, const double* replay, int* worst) {
     const size_t ncf = (size_t)c->L.N0 * c->L.NZ;
     c->lknown = c->ln;
     c->flag_ab = 0;
@@ -591,7 +640,11 @@ int rk3_step(nsmp_ctx* c, double* keep, int* worst) {
                                    c->stream));
         }
         nsmp_stage_info inf{};
+        c->tape_x = tape ? tape + (size_t)st * c->mesh.nprism : nullptr;
+        c->replay_x = replay ? replay + (size_t)st * c->mesh.nprism : nullptr;
         int rc = run_stage(c, 3, &inf);
+        c->tape_x = nullptr;
+        c->replay_x = nullptr;
         if (rc < 0) return rc;
         *worst = std::max(*worst, rc);
         if (st == 1) {
@@ -634,10 +687,12 @@ int adj_stage(nsmp_ctx* c, const double* in, double* const* Aout, double* const*
     CK(cudaMemsetAsync(S.avx[3], 0, nvx * sizeof(double), st));
     // mean removals and the solve
     LAUNCH(NSMP_K_OTHER, k_adj_sum<<<gp, kBlock, 0, st>>>(m, S.apc, c->red, c->d_scal));
-    LAUNCH(NSMP_K_OTHER, k_adj_solve_rhs<<<gp, kBlock, 0, st>>>(m, S.apc, c->rhsp, S.hsum, c->d_scal));
+    LAUNCH(NSMP_K_OTHER, k_adj_solve_rhs<<<gp, kBlock, 0, st>>>(m, S.apc, c->rhsp, S.hsum, c->red, c->d_scal));
+    LAUNCH(NSMP_K_OTHER, k_adj_unit<<<gp, kBlock, 0, st>>>(m, c->rhsp, c->d_scal));
     CKL("adjoint pressure right-hand side");
+    LAUNCH(NSMP_K_OTHER, k_adj_guess<<<gp, kBlock, 0, st>>>(m, S.lamc, S.guess, c->d_scal));
     const double* lam = nullptr;
-    int rc = run_pressure_fp64(c, S.zero, &lam);
+    int rc = run_pressure_fp64(c, S.guess, &lam);
     if (rc < 0) return rc;
     CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -649,6 +704,7 @@ int adj_stage(nsmp_ctx* c, const double* in, double* const* Aout, double* const*
     rc = std::max(rc, c->h_scal->status);
     LAUNCH(NSMP_K_OTHER, k_adj_sum<<<gp, kBlock, 0, st>>>(m, lam, c->red, c->d_scal));
     LAUNCH(NSMP_K_OTHER, k_adj_center<<<gp, kBlock, 0, st>>>(m, lam, S.arhs, c->d_scal));
+    LAUNCH(NSMP_K_OTHER, k_adj_keep<<<gp, kBlock, 0, st>>>(m, lam, S.lamc, c->d_scal));
     // face pass
     AdjFaceArgs fa{S.arhs, Aout[4], Aout[5], Aout[6], Aout[7], Aout[8], S.aus[0], S.aus[1], S.aus[2], S.avx[3],
                    1.0 / P.dt};
@@ -759,10 +815,15 @@ int run_adjoint(nsmp_ctx* c, int nsteps, int ckpt_every, const double* fx, doubl
     const int nseg = (nsteps + ckpt_every - 1) / ckpt_every;
     rc = run_set_body_force(c, fx);
     if (rc) return rc;
-    // checkpoints (state at the start of every segment and at the end) and
-    // the stage inputs of one segment
-    DevBuf ck, seg;
-    cudaError_t e = cudaMalloc((void**)&ck.p, (size_t)(nseg + 1) * NF_STATE * ncf * sizeof(double));
+    cudaError_t e = cudaSuccess;
+    // checkpoints (state at the start of every segment and at the end), the
+    // stage inputs of one segment, and the PPE solution of every stage (the
+    // recomputation of a segment replays those instead of solving again)
+    DevBuf ck, seg, tape;
+    const size_t np3 = (size_t)3 * m.nprism;
+    e = cudaMalloc((void**)&tape.p, (size_t)nsteps * np3 * sizeof(double));
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc(adjoint pressure tape)");
+    e = cudaMalloc((void**)&ck.p, (size_t)(nseg + 1) * NF_STATE * ncf * sizeof(double));
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc(adjoint checkpoints)");
     e = cudaMalloc((void**)&seg.p, (size_t)ckpt_every * 3 * 8 * ncf * sizeof(double));
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc(adjoint segment)");
@@ -776,7 +837,7 @@ int run_adjoint(nsmp_ctx* c, int nsteps, int ckpt_every, const double* fx, doubl
             rc = copy_state(c, ck.p + (size_t)(n / ckpt_every) * NF_STATE * ncf, true);
             if (rc) return rc;
         }
-        rc = rk3_step(c, nullptr, &worst);
+        rc = rk3_step(c, nullptr, tape.p + (size_t)n * np3, nullptr, &worst);
         if (rc) return rc;
         double tau;
         rc = wall_shear_now(c, &tau);
@@ -791,13 +852,14 @@ int run_adjoint(nsmp_ctx* c, int nsteps, int ckpt_every, const double* fx, doubl
     double* const* B = S.A[1];
     for (int f = 0; f < NF_STATE; ++f) CK(cudaMemsetAsync(A[f], 0, ncf * sizeof(double), st));
     CK(cudaMemsetAsync(S.afx, 0, ncf * sizeof(double), st));
+    CK(cudaMemsetAsync(S.lamc, 0, ncf * sizeof(double), st));
     const int gc = grid_for(c, m.N0), ga = grid_for(c, (long long)ncf);
     for (int sgi = nseg - 1; sgi >= 0; --sgi) {
         const int n0 = sgi * ckpt_every, n1 = std::min(nsteps, n0 + ckpt_every);
         rc = copy_state(c, ck.p + (size_t)sgi * NF_STATE * ncf, false);
         if (rc) return rc;
         for (int n = n0; n < n1; ++n) {
-            rc = rk3_step(c, seg.p + (size_t)(n - n0) * 3 * 8 * ncf, &worst);
+            rc = rk3_step(c, seg.p + (size_t)(n - n0) * 3 * 8 * ncf, nullptr, tape.p + (size_t)n * np3, &worst);
             if (rc) return rc;
         }
         for (int n = n1 - 1; n >= n0; --n) {

@@ -50,6 +50,11 @@ struct nsmp_ctx {
     int last_outer = 0;
     double* stage_buf = nullptr;  // (N_CELL,NZ) staging for transfers
     double* fx = nullptr;         // body force on u (cell layout), null when unset
+    // pressure tape of the adjoint: when tape_x is set a stage copies its
+    // PPE solution there; when replay_x is set a stage uses that solution
+    // instead of solving (recomputation of a checkpointed segment)
+    double* tape_x = nullptr;
+    const double* replay_x = nullptr;
     struct AdjScratch* adj = nullptr;  // discrete-adjoint work buffers (lazily allocated)
     // reductions and scalars
     nsmp::RedScratch red{}, red2{};

@@ -24,6 +24,7 @@ struct Scal {
     double b1, b2, r1, r2, e1, e2;
     double diag[4];
     double jval, jsum;     // wall-shear objective, adjoint mean-removal sum
+    double adjn;           // |rhs|_2 of the adjoint pressure solve
     int iter, done, converged, status;
     int max_iters, pad;
     double eps;

@@ -523,8 +523,16 @@ int run_stage(nsmp_ctx* c, int fin_rk, nsmp_stage_info* info) {
     LAUNCH(NSMP_K_FACES_DIV, k_faces_div<<<grid_occ(c, k_faces_div, m.nprism), kBlock, 0, st>>>(m, fa, c->red, c->d_scal));
     CKL("k_faces_div");
     const double* xsol = nullptr;
-    const int rcp = (c->precision == NSMP_MIXED) ? run_pressure_mixed(c, K[3], &xsol) : run_pressure_fp64(c, K[3], &xsol);
-    if (rcp) return rcp;
+    const bool replay = c->replay_x != nullptr;
+    if (replay) {
+        xsol = c->replay_x;
+    } else {
+        const int rcp = (c->precision == NSMP_MIXED) ? run_pressure_mixed(c, K[3], &xsol)
+                                                     : run_pressure_fp64(c, K[3], &xsol);
+        if (rcp) return rcp;
+        if (c->tape_x)
+            CK(cudaMemcpyAsync(c->tape_x, xsol, sizeof(double) * m.nprism, cudaMemcpyDeviceToDevice, st));
+    }
     LAUNCH(NSMP_K_PMEAN, k_pmean<<<grid_occ(c, k_pmean, m.nprism), kBlock, 0, st>>>(m, xsol, c->red, c->d_scal));
     CKL("k_pmean");
     LAUNCH(NSMP_K_VERTEX1, k_vertex1<<<grid_occ(c, k_vertex1, (long long)m.nclass * m.NZI), kBlock, 0, st>>>(m, xsol, c->d_scal, c->vtx[3]));
@@ -536,6 +544,14 @@ int run_stage(nsmp_ctx* c, int fin_rk, nsmp_stage_info* info) {
     CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     prof_resolve(c);
+    if (replay) {  // the solve was replayed from the tape: no solver statistics
+        nsmp_stage_info inf{};
+        inf.converged = 1;
+        inf.max_eddy = P.les ? c->h_scal->max_eddy : 0.0;
+        c->last = inf;
+        if (info) *info = inf;
+        return 0;
+    }
     const Scal& s = *c->h_scal;
     c->last_iters = s.iter > 0 ? s.iter : 1;
     c->bicg_iters += s.iter;

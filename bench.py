@@ -494,14 +494,15 @@ def run_adjoint_bench(args):
     l2, i2 = s.counters()
     ncf = n0 * nz
     nseg = -(-N // K)
-    dev_bytes = 8 * ncf * (30 + 9 * (nseg + 1) + 24 * K)
+    dev_bytes = 8 * ncf * (30 + 9 * (nseg + 1) + 24 * K) + 8 * 3 * prisms * N
     line = {"metric": "adjoint/forward time", "value": t_adj / t_fwd, "unit": "x", "higher_is_better": False,
             "workload": workload_desc(args.workload), "prisms": prisms, "steps": N, "ckpt_every": K,
             "forward_s": t_fwd, "adjoint_s": t_adj, "J": J, "grad_l2": float(np.linalg.norm(grad)),
             "status": rc, "bicgstab_iters_forward": i1 - i0, "bicgstab_iters_adjoint_call": i2 - i1,
             "adjoint_device_bytes": dev_bytes,
             "adjoint_device_bytes_note": "work buffers of nsmp_adjoint (30 cell fields + 9 per checkpoint + 24 per "
-                                         "step of one segment), on top of the context's forward state",
+                                         "step of one segment + the pressure tape, 3 solutions per step), on top "
+                                         "of the context's forward state",
             "gpu_launches": l2 - l1, "dtype": "f64"}
     print(json.dumps(line), flush=True)
     s.close()

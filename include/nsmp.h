@@ -180,10 +180,12 @@ int nsmp_wall_shear(nsmp_ctx* ctx, double* tau);
  * nsmp_set_body_force), J = mean over steps 1..nsteps of nsmp_wall_shear,
  * and the gradient dJ/dfx, (N0,NZ) like fx, by the discrete adjoint of the
  * steps.  The state is checkpointed every ckpt_every steps and each segment
- * is recomputed once during the reverse sweep (device memory: 9 cell fields
- * per checkpoint plus 24 per step of one segment).  The context ends at the
- * state after the nsteps steps with fx still set.  Returns the worst status
- * of the forward and adjoint pressure solves. */
+ * is recomputed once during the reverse sweep, replaying the pressure
+ * solutions recorded by the forward sweep instead of solving again (device
+ * memory: 9 cell fields per checkpoint, 24 per step of one segment, and 3
+ * interior fields per step for the recorded pressures).  The context ends at
+ * the state after the nsteps steps with fx still set.  Returns the worst
+ * status of the forward and adjoint pressure solves. */
 int nsmp_adjoint(nsmp_ctx* ctx, int nsteps, int ckpt_every, const double* fx,
                  double* grad_out, double* J_out);
 /* y = A x and y = A^T x for the PPE operator (PDE.F90:69-121) on interior

@@ -58,6 +58,8 @@ enum { TagBCu = 1, TagBCv = 2, TagBCw = 3, TagBCp = 0 };
 
 struct orc_ctx {
     orc_params P;
+    int has_fx = 0;
+    R2 fx;               // body force on u, (N0,NZ) (extension)
     int N0, NV, NZ, NC;  // N_CELL0, N_VERT, NZ, N_CELL (= N_CELLexact)
     double Lsig;         // SigFin - SigIni
     // mesh
@@ -1156,6 +1158,10 @@ void hydro(orc_ctx& c, int fin_rk) {
             Gam(i, k) = P.les ? c.eddy(i, k) + invRe : invRe;
             rhsu(i, k) = P.bdx; rhsv(i, k) = P.bdy; rhsw(i, k) = P.bdz;
         }
+    if (c.has_fx)  // body force on u (extension; the reference has bdx only)
+#pragma omp parallel for schedule(static)
+        for (int k = 2; k <= NZ - 1; ++k)
+            for (int i = 1; i <= N0; ++i) rhsu(i, k) = P.bdx + c.fx(i, k);
     ufstar = c.uf; vfstar = c.vf; wfstar = c.wf;
     AdvDiffNS(c, rhsu, rhsv, rhsw, c.uf, c.vf, c.wf, Gam, Gam, Gam);
 #pragma omp parallel for schedule(static)
@@ -1358,6 +1364,15 @@ int orc_step(orc_ctx* c, int fin_rk, orc_info* info) {
     c->ufn = c->ufnp; c->vfn = c->vfnp; c->wfn = c->wfnp; c->pfn = c->pfnp;
     if (info) { *info = c->info; info->iters = max_it; }
     return c->info.converged ? 0 : 1;
+}
+
+// Body force on u, (N0,NZ) column-major; NULL removes it.
+int orc_set_body_force(orc_ctx* c, const double* fx) {
+    if (!fx) { c->has_fx = 0; return 0; }
+    c->fx.init(c->N0, c->NZ);
+    std::memcpy(c->fx.d.data(), fx, sizeof(double) * (size_t)c->N0 * c->NZ);
+    c->has_fx = 1;
+    return 0;
 }
 
 int orc_apply_A(orc_ctx* c, const double* x, double* y) {

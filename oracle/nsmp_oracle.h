@@ -99,6 +99,7 @@ void orc_set_flag_ab(orc_ctx* c, int f);
 int orc_step(orc_ctx* c, int fin_rk, orc_info* info);
 
 /* Operator hooks for unit parity tests. */
+int orc_set_body_force(orc_ctx* c, const double* fx);      /* (N0,NZ), NULL: none */
 int orc_apply_A(orc_ctx* c, const double* x, double* y);   /* (N_CELL,NZ) -> (N0..)*/
 int orc_gradient_lsm(orc_ctx* c, const double* f, double* dfdx, double* dfdy,
                      double* dfds);                         /* (N_CELL,NZ) each   */

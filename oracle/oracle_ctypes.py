@@ -65,6 +65,7 @@ def lib():
         L.orc_set.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         L.orc_step.argtypes = [C.c_void_p, C.c_int, P(OrcInfo)]
         L.orc_apply_A.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_set_body_force.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_gradient_lsm.argtypes = [C.c_void_p] + [C.c_void_p] * 4
         L.orc_vertex_interp.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
         L.orc_mass_diag.argtypes = [C.c_void_p, C.c_void_p]
@@ -155,6 +156,13 @@ class Oracle:
     @flag_ab.setter
     def flag_ab(self, f):
         lib().orc_set_flag_ab(self.h, int(f))
+
+    def set_body_force(self, fx):
+        if fx is None:
+            lib().orc_set_body_force(self.h, None)
+            return
+        self._fx = np.asfortranarray(fx, dtype=np.float64)
+        lib().orc_set_body_force(self.h, _ptr(self._fx))
 
     def apply_A(self, x):
         x = np.asfortranarray(x, dtype=np.float64)

@@ -114,6 +114,21 @@ def test_config0_one_step_rk3():
     _compare(o, s, 1e-11, "config0 1 step")
 
 
+def test_body_force_rk3_against_oracle():
+    """A seeded per-cell body force on u (the adjoint's control) in the
+    forward stage: two RK3 steps against the oracle with the same force."""
+    prm, mesh = small_case(8, 6, layers=6, eps=TIGHT, max_iters=2000)
+    o, s = _pair(prm, mesh)
+    fx = np.zeros((prm["n0"], prm["nz"]), order="F")
+    fx[:, 1:-1] = 0.5 * np.random.default_rng(2).standard_normal((prm["n0"], prm["nz"] - 2))
+    o.set_body_force(fx)
+    s.set_body_force(fx)
+    for _ in range(2):
+        o.step(3)
+        s.step(3, 1)
+    _compare(o, s, 1e-10, "body force")
+
+
 @pytest.mark.parametrize("fin_rk,nsteps", [(1, 4), (2, 3), (3, 2)])
 def test_integrators(fin_rk, nsteps):
     """Euler->AB2 (1.55/-0.55, hydro.F90:225-231), Heun RK2 (nsmp3D.F90:531-546), SSP-RK3."""

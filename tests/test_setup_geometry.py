@@ -102,3 +102,22 @@ def test_oracle_ppe_symmetric_pattern():
     lhs = float(np.sum(av * w[:o.n0, 1:-1]))
     rhs = float(np.sum(v[:o.n0, 1:-1] * aw))
     assert abs(lhs - rhs) <= 1e-10 * max(abs(lhs), 1.0)
+
+
+def test_oracle_body_force_zero_and_nonzero():
+    """The oracle's body-force hook: a zero force changes no bit; a uniform
+    push along x raises the mean of u."""
+    from oracle import oracle_ctypes as oc
+    prm, mesh = small_case(6, 4, layers=4, eps=1e-12)
+    runs = []
+    for fx in (None, 0.0, 5.0):
+        o = oc.Oracle(oracle_params(prm), mesh, nthreads=2)
+        u, v, w, p = ng.initial_channel(prm, o.ncell, seed=1)
+        o.user_initial(u, v, w, p)
+        if fx is not None:
+            o.set_body_force(np.full((prm["n0"], prm["nz"]), fx, order="F"))
+        o.step(3)
+        runs.append(o.get(oc.F_U))
+    assert np.array_equal(runs[0], runs[1])
+    n0 = prm["n0"]
+    assert runs[2][:n0, 1:-1].mean() > runs[0][:n0, 1:-1].mean()
