@@ -21,7 +21,10 @@
 // solution of every stage (the pressure tape); during the reverse sweep one
 // segment is recomputed from its checkpoint, replaying the taped pressures
 // instead of solving again, and the inputs of each of its stages (u, v, w
-// with ghost layers and the five face fluxes) are kept.
+// with ghost layers and the five face fluxes) are kept -- for the whole
+// segment when that fits, else for the step being reversed, re-reached from
+// inner checkpoints.  The adjoint pressure solves run in the context's
+// precision mode (FP64, or FP32 BiCGSTAB with FP64 refinement).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -47,6 +50,7 @@ struct AdjScratch {
     int* tcls = nullptr;
     double* tcoef = nullptr;
     double tot_area = 0.0, hsum = 0.0;
+    double seg_budget = 0.0;  // bytes for the segment's stage inputs; 0: 80 % of free memory
 };
 
 namespace nsmp {
@@ -692,7 +696,7 @@ int adj_stage(nsmp_ctx* c, const double* in, double* const* Aout, double* const*
     CKL("adjoint pressure right-hand side");
     LAUNCH(NSMP_K_OTHER, k_adj_guess<<<gp, kBlock, 0, st>>>(m, S.lamc, S.guess, c->d_scal));
     const double* lam = nullptr;
-    int rc = run_pressure_fp64(c, S.guess, &lam);
+    int rc = (c->precision == NSMP_MIXED) ? run_pressure_mixed(c, S.guess, &lam) : run_pressure_fp64(c, S.guess, &lam);
     if (rc < 0) return rc;
     CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -739,6 +743,8 @@ struct DevBuf {  // per-call device buffer
 };
 
 }  // namespace
+
+int adj_ensure(nsmp_ctx* c) { return adj_alloc(c); }
 
 void adj_free(nsmp_ctx* c) {
     delete c->adj;  // device buffers are in c->allocs
@@ -825,8 +831,26 @@ int run_adjoint(nsmp_ctx* c, int nsteps, int ckpt_every, const double* fx, doubl
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc(adjoint pressure tape)");
     e = cudaMalloc((void**)&ck.p, (size_t)(nseg + 1) * NF_STATE * ncf * sizeof(double));
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc(adjoint checkpoints)");
-    e = cudaMalloc((void**)&seg.p, (size_t)ckpt_every * 3 * 8 * ncf * sizeof(double));
+    // The stage inputs of a whole segment (24 cell fields per step) when they
+    // fit in 80 % of the free device memory; else inner checkpoints every q
+    // steps of the segment (q ~ sqrt(ckpt_every)) and the stage inputs of the
+    // one step being reversed, each step re-reached by replaying at most
+    // q - 1 steps (replays skip the PPE solve: ~5 % of a step each).
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const size_t seg_all = (size_t)ckpt_every * 3 * 8 * ncf * sizeof(double);
+    const double budget = S.seg_budget > 0.0 ? S.seg_budget : 0.8 * (double)free_b;
+    const bool inner = (double)seg_all > budget;
+    int q = 1;
+    while ((long long)q * q < ckpt_every) ++q;
+    const int ninner = (ckpt_every + q - 1) / q;
+    if (!inner) {
+        e = cudaMalloc((void**)&seg.p, seg_all);
+    } else {
+        e = cudaMalloc((void**)&seg.p, ((size_t)ninner * NF_STATE + 3 * 8) * ncf * sizeof(double));
+    }
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc(adjoint segment)");
+    double* inner_ck = inner ? seg.p + (size_t)3 * 8 * ncf : nullptr;
     double wb, wt;
     shear_weights(c, wb, wt);
     // forward sweep
@@ -859,11 +883,27 @@ int run_adjoint(nsmp_ctx* c, int nsteps, int ckpt_every, const double* fx, doubl
         rc = copy_state(c, ck.p + (size_t)sgi * NF_STATE * ncf, false);
         if (rc) return rc;
         for (int n = n0; n < n1; ++n) {
-            rc = rk3_step(c, seg.p + (size_t)(n - n0) * 3 * 8 * ncf, nullptr, tape.p + (size_t)n * np3, &worst);
+            if (inner && (n - n0) % q == 0) {
+                rc = copy_state(c, inner_ck + (size_t)((n - n0) / q) * NF_STATE * ncf, true);
+                if (rc) return rc;
+            }
+            double* keep = inner ? nullptr : seg.p + (size_t)(n - n0) * 3 * 8 * ncf;
+            rc = rk3_step(c, keep, nullptr, tape.p + (size_t)n * np3, &worst);
             if (rc) return rc;
         }
         for (int n = n1 - 1; n >= n0; --n) {
-            const double* keep = seg.p + (size_t)(n - n0) * 3 * 8 * ncf;
+            const double* keep = seg.p + (size_t)(inner ? 0 : n - n0) * 3 * 8 * ncf;
+            if (inner) {  // re-reach step n from the inner checkpoint below it
+                const int j = (n - n0) / q;
+                rc = copy_state(c, inner_ck + (size_t)j * NF_STATE * ncf, false);
+                if (rc) return rc;
+                for (int n2 = n0 + j * q; n2 < n; ++n2) {
+                    rc = rk3_step(c, nullptr, nullptr, tape.p + (size_t)n2 * np3, &worst);
+                    if (rc) return rc;
+                }
+                rc = rk3_step(c, seg.p, nullptr, tape.p + (size_t)n * np3, &worst);
+                if (rc) return rc;
+            }
             // objective at u^{n+1}
             k_adj_seed<<<gc, kBlock, 0, st>>>(m, A[0], wb / nsteps, wt / nsteps);
             CKL("k_adj_seed");
@@ -916,6 +956,16 @@ int nsmp_set_body_force(nsmp_ctx* c, const double* fx) {
 int nsmp_wall_shear(nsmp_ctx* c, double* tau) {
     if (!c || !tau) return NSMP_ERR_ARG;
     return nsmp::run_wall_shear(c, tau);
+}
+
+int nsmp_set_adjoint_budget(nsmp_ctx* c, double bytes) {
+    if (!c || bytes < 0.0) return NSMP_ERR_ARG;
+    if (!c->adj) {
+        int rc = nsmp::adj_ensure(c);
+        if (rc) return rc;
+    }
+    c->adj->seg_budget = bytes;
+    return NSMP_OK;
 }
 
 int nsmp_apply_A(nsmp_ctx* c, const double* x, double* y) {

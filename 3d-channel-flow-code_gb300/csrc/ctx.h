@@ -104,6 +104,7 @@ int run_apply_A(nsmp_ctx* c, int transpose, const double* x, double* y);
 int run_set_body_force(nsmp_ctx* c, const double* fx);
 int run_wall_shear(nsmp_ctx* c, double* tau);
 void adj_free(nsmp_ctx* c);
+int adj_ensure(nsmp_ctx* c);
 int prof_begin(nsmp_ctx* c, int kid);   // returns event slot or -1
 void prof_end(nsmp_ctx* c, int slot);
 int prof_resolve(nsmp_ctx* c);

@@ -63,6 +63,7 @@ EXPORTS = [
     "nsmp_sigma_grid", "nsmp_geometry", "nsmp_prof_enable", "nsmp_prof_read", "nsmp_counters",
     "nsmp_set_inner_solver", "nsmp_solver_log", "nsmp_mass_diag_noalloc",
     "nsmp_set_body_force", "nsmp_wall_shear", "nsmp_adjoint", "nsmp_apply_A", "nsmp_apply_AT",
+    "nsmp_set_adjoint_budget",
 ]
 
 (K_VERTEX4, K_STAGE_RHS, K_FACES_DIV, K_BICG_INIT, K_BICG_P, K_BICG_SPMV_V, K_BICG_S, K_BICG_SPMV_T,
@@ -113,6 +114,7 @@ def lib(build_if_missing=True):
     L.nsmp_wall_shear.argtypes = [vp, P(C.c_double)]
     L.nsmp_adjoint.argtypes = [vp, C.c_int, C.c_int, vp, vp, P(C.c_double)]
     L.nsmp_apply_A.argtypes = [vp, vp, vp]
+    L.nsmp_set_adjoint_budget.argtypes = [vp, C.c_double]
     L.nsmp_apply_AT.argtypes = [vp, vp, vp]
     L.nsmp_stream.argtypes = [vp]
     L.nsmp_stream.restype = vp
@@ -328,6 +330,10 @@ class Solver:
         J = C.c_double()
         rc = self._check(self.L.nsmp_adjoint(self.h, int(nsteps), int(ckpt_every), _p(fx), _p(grad), C.byref(J)))
         return J.value, grad, rc
+
+    def set_adjoint_budget(self, nbytes):
+        """Bytes for the stage inputs of an adjoint segment (0: automatic)."""
+        self._check(self.L.nsmp_set_adjoint_budget(self.h, float(nbytes)))
 
     def apply_A(self, x, transpose=False):
         x = self._n0nz(x)

@@ -460,7 +460,8 @@ def run_adjoint_bench(args):
     nx, ny, layers, dt = WORKLOADS[args.workload]
     prisms = 2 * nx * ny * layers
     mesh = ng.make_mesh(nx, ny)
-    prm = ng.channel_params(nx, ny, layers, dt, precision=ng.FP64)
+    mixed = args.precision == "mixed"
+    prm = ng.channel_params(nx, ny, layers, dt, precision=(ng.MIXED if mixed else ng.FP64))
     s = ng.Solver(prm, mesh)
     u0, v0, w0, p0 = ng.initial_channel(prm, s.ncell, seed=1)
     s.user_initial(u0, v0, w0, p0)
@@ -483,6 +484,7 @@ def run_adjoint_bench(args):
         return e0.elapsed_time(e1) / 1e3, out
 
     s.set_body_force(fx)
+    s.set_adjoint_budget(args.adjoint_budget_gb * 1e9)
     s.upload_state(*cells, faces, hist, 0)
     s.step(3, 1)  # warm-up (first-use allocations, occupancy queries)
     s.upload_state(*cells, faces, hist, 0)
@@ -490,7 +492,21 @@ def run_adjoint_bench(args):
     t_fwd, _ = timed(lambda: [s.step(3, 1) for _ in range(N)])
     l1, i1 = s.counters()
     s.upload_state(*cells, faces, hist, 0)
+    # device memory in use while the adjoint runs (sampled every 50 ms)
+    free_min = [torch.cuda.mem_get_info()[0]]
+    total = torch.cuda.mem_get_info()[1]
+    stop = threading.Event()
+
+    def poll():
+        while not stop.is_set():
+            free_min[0] = min(free_min[0], torch.cuda.mem_get_info()[0])
+            time.sleep(0.05)
+
+    th = threading.Thread(target=poll, daemon=True)
+    th.start()
     t_adj, (J, grad, rc) = timed(lambda: s.adjoint(N, K, fx))
+    stop.set()
+    th.join()
     l2, i2 = s.counters()
     ncf = n0 * nz
     nseg = -(-N // K)
@@ -503,7 +519,10 @@ def run_adjoint_bench(args):
             "adjoint_device_bytes_note": "work buffers of nsmp_adjoint (30 cell fields + 9 per checkpoint + 24 per "
                                          "step of one segment + the pressure tape, 3 solutions per step), on top "
                                          "of the context's forward state",
-            "gpu_launches": l2 - l1, "dtype": "f64"}
+            "peak_device_bytes_in_use": total - free_min[0],
+            "segment_budget_bytes": args.adjoint_budget_gb * 1e9 or "80% of free memory",
+            "gpu_launches": l2 - l1, "dtype": "f32+f64" if mixed else "f64",
+            "precision": "mixed forward and adjoint solves, FP64 adjoint accumulation" if mixed else "fp64"}
     print(json.dumps(line), flush=True)
     s.close()
     return 0
@@ -525,6 +544,8 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=0,
                     help="instead of timing the forward: adjoint/forward cost over N FP64 RK3 steps")
     ap.add_argument("--ckpt", type=int, default=20, help="checkpoint spacing of --adjoint-steps")
+    ap.add_argument("--adjoint-budget-gb", type=float, default=0.0,
+                    help="device memory for the stage inputs of an adjoint segment (0: automatic)")
     args = ap.parse_args()
     if args.accuracy_steps > 0:
         return run_accuracy(args)

@@ -181,13 +181,20 @@ int nsmp_wall_shear(nsmp_ctx* ctx, double* tau);
  * and the gradient dJ/dfx, (N0,NZ) like fx, by the discrete adjoint of the
  * steps.  The state is checkpointed every ckpt_every steps and each segment
  * is recomputed once during the reverse sweep, replaying the pressure
- * solutions recorded by the forward sweep instead of solving again (device
- * memory: 9 cell fields per checkpoint, 24 per step of one segment, and 3
- * interior fields per step for the recorded pressures).  The context ends at
- * the state after the nsteps steps with fx still set.  Returns the worst
- * status of the forward and adjoint pressure solves. */
+ * solutions recorded by the forward sweep instead of solving again.  Device
+ * memory: 9 cell fields per checkpoint, 3 interior fields per step for the
+ * recorded pressures, and the stage inputs of a segment (24 cell fields per
+ * step) -- or, when those exceed the budget of nsmp_set_adjoint_budget,
+ * inner checkpoints every ~sqrt(ckpt_every) steps of the segment plus the
+ * stage inputs of one step.  The adjoint pressure solves run in the
+ * context's precision mode.  The context ends at the state after the nsteps
+ * steps with fx still set.  Returns the worst status of the forward and
+ * adjoint pressure solves. */
 int nsmp_adjoint(nsmp_ctx* ctx, int nsteps, int ckpt_every, const double* fx,
                  double* grad_out, double* J_out);
+/* Bytes nsmp_adjoint may use for the stage inputs of a segment; 0 (the
+ * default) means 80 % of the free device memory at the call. */
+int nsmp_set_adjoint_budget(nsmp_ctx* ctx, double bytes);
 /* y = A x and y = A^T x for the PPE operator (PDE.F90:69-121) on interior
  * fields (N0,NZ): the hooks of the dot-product test <A v, w> = <v, A^T w>. */
 int nsmp_apply_A(nsmp_ctx* ctx, const double* x, double* y);

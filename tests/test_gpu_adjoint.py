@@ -138,3 +138,39 @@ def test_adjoint_checkpoint_spacing_does_not_change_the_gradient():
         assert J == out[0][0]
         assert np.linalg.norm(g - out[0][1]) <= 1e-6 * np.linalg.norm(out[0][1])
     s.close()
+
+
+def test_adjoint_inner_checkpoints_match_the_segment_store():
+    """A budget too small for the stage inputs of a whole segment switches
+    nsmp_adjoint to inner checkpoints; J is bitwise the same and the gradient
+    agrees to the adjoint solve accuracy."""
+    prm, mesh, s = _solver()
+    n0, nz = prm["n0"], prm["nz"]
+    fx = _interior_random(np.random.default_rng(2), n0, nz, 0.01)
+    st = _state(s)
+    out = []
+    for budget in (0, 1):
+        s.set_adjoint_budget(budget)
+        s.upload_state(*st[0], st[1], st[2], 0)
+        J, g, rc = s.adjoint(5, 5, fx)
+        assert rc == 0
+        out.append((J, g))
+    assert out[1][0] == out[0][0]
+    assert np.linalg.norm(out[1][1] - out[0][1]) <= 1e-6 * np.linalg.norm(out[0][1])
+    s.close()
+
+
+def test_adjoint_in_mixed_precision_agrees_with_fp64():
+    prm, mesh, s = _solver()
+    n0, nz = prm["n0"], prm["nz"]
+    fx = _interior_random(np.random.default_rng(2), n0, nz, 0.01)
+    st = _state(s)
+    J64, g64, rc = s.adjoint(3, 2, fx)
+    assert rc == 0
+    s.set_precision(ng.MIXED)
+    s.upload_state(*st[0], st[1], st[2], 0)
+    J32, g32, rc = s.adjoint(3, 2, fx)
+    assert rc == 0
+    assert abs(J32 - J64) <= 1e-9 * abs(J64)
+    assert np.linalg.norm(g32 - g64) <= 1e-6 * np.linalg.norm(g64)
+    s.close()
