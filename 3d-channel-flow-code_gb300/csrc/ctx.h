@@ -44,6 +44,7 @@ struct nsmp_ctx {
     float *r32 = nullptr, *r032 = nullptr, *p32[2] = {}, *v32[2] = {}, *s32 = nullptr, *t32 = nullptr,
           *e32 = nullptr, *invD32 = nullptr, *lev32 = nullptr;
     nsmp::ColPPE32* d_ppe32 = nullptr;
+    int l2_limit_set = 0;         // 1: this context raised the persisting-L2 limit (reset at destroy)
     double inner_tol = 1e-1;      // FP32 residual reduction that triggers an FP64 update
     int inner_cap = 50;           // most FP32 iterations between two FP64 updates
     int restart_every = 300;      // most FP32 iterations of one Krylov process
@@ -56,6 +57,7 @@ struct nsmp_ctx {
     double* tape_x = nullptr;
     const double* replay_x = nullptr;
     struct AdjScratch* adj = nullptr;  // discrete-adjoint work buffers (lazily allocated)
+    struct StatState* stats = nullptr; // turbulence-statistics sums (lazily allocated)
     // reductions and scalars
     nsmp::RedScratch red{}, red2{};
     nsmp::Scal* d_scal = nullptr;
@@ -104,6 +106,7 @@ int run_apply_A(nsmp_ctx* c, int transpose, const double* x, double* y);
 int run_set_body_force(nsmp_ctx* c, const double* fx);
 int run_wall_shear(nsmp_ctx* c, double* tau);
 void adj_free(nsmp_ctx* c);
+void stats_free(nsmp_ctx* c);
 int adj_ensure(nsmp_ctx* c);
 int prof_begin(nsmp_ctx* c, int kid);   // returns event slot or -1
 void prof_end(nsmp_ctx* c, int slot);

@@ -549,9 +549,13 @@ int mixed_alloc(nsmp_ctx* c) {
         return e;
     };
     for (double** p : {&c->b64, &c->xa, &c->xb}) CK(dalloc((void**)p, ncf * sizeof(double)));
-    for (float** p : {&c->r32, &c->r032, &c->p32[0], &c->p32[1], &c->v32[0], &c->v32[1], &c->s32, &c->t32,
-                      &c->e32, &c->invD32})
+    for (float** p : {&c->r32, &c->p32[0], &c->p32[1], &c->v32[0], &c->v32[1], &c->s32, &c->t32, &c->e32})
         CK(dalloc((void**)p, ncf * sizeof(float)));
+    // D^-1 and the shadow residual are read by both passes of every
+    // iteration and never written inside a Krylov process: one block, so a
+    // single L2 access-policy window can keep them resident
+    CK(dalloc((void**)&c->invD32, 2 * ncf * sizeof(float)));
+    c->r032 = c->invD32 + ncf;
     CK(dalloc((void**)&c->d_ppe32, sizeof(ColPPE32) * L.N0));
     CK(dalloc((void**)&c->lev32, sizeof(float) * 3 * L.NZ));
     std::vector<ColPPE32> p32(L.N0);
@@ -577,9 +581,53 @@ int mixed_alloc(nsmp_ctx* c) {
     return 0;
 }
 
+// L2 residency of D^-1 and r0 (the contiguous block of mixed_alloc) for the
+// kernels of one mixed solve: persisting up to the set-aside the device
+// allows, streaming beyond it.  off() returns the stream and the persisting
+// lines to normal use.
+struct L2Window {
+    nsmp_ctx* c;
+    bool on = false;
+    L2Window(nsmp_ctx* cc, size_t bytes) : c(cc) {
+        int dev = 0, maxwin = 0, maxpers = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) return;
+        cudaDeviceGetAttribute(&maxwin, cudaDevAttrMaxAccessPolicyWindowSize, dev);
+        cudaDeviceGetAttribute(&maxpers, cudaDevAttrMaxPersistingL2CacheSize, dev);
+        if (maxwin <= 0 || maxpers <= 0) return;
+        const size_t win = std::min(bytes, (size_t)maxwin);
+        size_t lim = 0;
+        if (cudaDeviceGetLimit(&lim, cudaLimitPersistingL2CacheSize) != cudaSuccess) return;
+        if (lim < std::min(win, (size_t)maxpers)) {
+            if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min(win, (size_t)maxpers)) != cudaSuccess) {
+                cudaGetLastError();
+                return;
+            }
+            c->l2_limit_set = 1;
+        }
+        cudaDeviceGetLimit(&lim, cudaLimitPersistingL2CacheSize);
+        cudaStreamAttrValue v{};
+        v.accessPolicyWindow.base_ptr = c->invD32;
+        v.accessPolicyWindow.num_bytes = win;
+        v.accessPolicyWindow.hitRatio = (float)std::min(1.0, (double)lim / (double)win);
+        v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+        on = cudaStreamSetAttribute(c->stream, cudaStreamAttributeAccessPolicyWindow, &v) == cudaSuccess;
+        cudaGetLastError();  // an unsupported window is not an error of the solve
+    }
+    ~L2Window() {
+        if (!on) return;
+        cudaStreamAttrValue v{};
+        v.accessPolicyWindow.num_bytes = 0;
+        cudaStreamSetAttribute(c->stream, cudaStreamAttributeAccessPolicyWindow, &v);
+        cudaCtxResetPersistingL2Cache();
+        cudaGetLastError();
+    }
+};
+
 int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     const Mesh& m = c->mesh;
     cudaStream_t st = c->stream;
+    L2Window l2win(c, (size_t)m.nprism * sizeof(float) + (size_t)m.N0 * m.NZ * sizeof(float));
     if (m.NZI & 1) {
         c->err = "mixed precision needs an even number of layers";
         return NSMP_ERR_UNSUPPORTED;

@@ -718,6 +718,12 @@ int ctx_init_device(nsmp_ctx* c) {
 void ctx_free(nsmp_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     adj_free(c);
+    stats_free(c);
+    if (c->l2_limit_set) {  // the persisting-L2 set-aside is a context limit: give it back
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+        cudaGetLastError();
+    }
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     c->ev_pool.clear();
     for (void* p : c->allocs) cudaFree(p);

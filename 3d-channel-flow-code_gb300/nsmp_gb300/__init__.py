@@ -63,12 +63,14 @@ EXPORTS = [
     "nsmp_sigma_grid", "nsmp_geometry", "nsmp_prof_enable", "nsmp_prof_read", "nsmp_counters",
     "nsmp_set_inner_solver", "nsmp_solver_log", "nsmp_mass_diag_noalloc",
     "nsmp_set_body_force", "nsmp_wall_shear", "nsmp_adjoint", "nsmp_apply_A", "nsmp_apply_AT",
-    "nsmp_set_adjoint_budget",
+    "nsmp_set_adjoint_budget", "nsmp_stats_reset", "nsmp_stats_sample", "nsmp_stats_count",
+    "nsmp_stats_download", "nsmp_stats_plane",
 ]
 
 (K_VERTEX4, K_STAGE_RHS, K_FACES_DIV, K_BICG_INIT, K_BICG_P, K_BICG_SPMV_V, K_BICG_S, K_BICG_SPMV_T,
  K_BICG_X, K_PMEAN, K_VERTEX1, K_PROJECT, K_IN_PV, K_IN_ST, K_MIX_UPDATE, K_MIX_SCALE, K_OTHER,
  K_COUNT) = range(18)
+(S_U, S_V, S_W, S_P, S_U2, S_V2, S_W2, S_UV, S_VW, S_WU, S_P2, S_EDDY, NSTATS) = range(13)
 KERNEL_NAMES = ["k_vertex4", "k_stage_rhs", "k_faces_div", "k_bicg_init", "k_bicg_p", "k_bicg_spmv_v",
                 "k_bicg_s", "k_bicg_spmv_t", "k_bicg_x", "k_pmean", "k_vertex1", "k_project", "k_in_pv",
                 "k_in_st", "k_mix_update", "k_mix_scale", "other"]
@@ -115,6 +117,11 @@ def lib(build_if_missing=True):
     L.nsmp_adjoint.argtypes = [vp, C.c_int, C.c_int, vp, vp, P(C.c_double)]
     L.nsmp_apply_A.argtypes = [vp, vp, vp]
     L.nsmp_set_adjoint_budget.argtypes = [vp, C.c_double]
+    L.nsmp_stats_reset.argtypes = [vp]
+    L.nsmp_stats_sample.argtypes = [vp]
+    L.nsmp_stats_count.argtypes = [vp, P(C.c_int)]
+    L.nsmp_stats_download.argtypes = [vp, C.c_int, vp]
+    L.nsmp_stats_plane.argtypes = [vp, vp, P(C.c_double)]
     L.nsmp_apply_AT.argtypes = [vp, vp, vp]
     L.nsmp_stream.argtypes = [vp]
     L.nsmp_stream.restype = vp
@@ -301,6 +308,30 @@ class Solver:
         out = np.zeros(4, dtype=np.float64)
         self._check(self.L.nsmp_mass_diag(self.h, _p(out)))
         return out
+
+    # ---- turbulence statistics -------------------------------------------
+    def stats_reset(self):
+        self._check(self.L.nsmp_stats_reset(self.h))
+
+    def stats_sample(self):
+        self._check(self.L.nsmp_stats_sample(self.h))
+
+    def stats_count(self):
+        n = C.c_int()
+        self._check(self.L.nsmp_stats_count(self.h, C.byref(n)))
+        return n.value
+
+    def stats_download(self, which):
+        out = np.zeros((self.ncell, self.nz), order="F")
+        self._check(self.L.nsmp_stats_download(self.h, int(which), _p(out)))
+        return out
+
+    def stats_plane(self):
+        """((NZ-2) x 10 array: yplus, mean u v w, rms u v w, shear uv vw wu), tke."""
+        out = np.zeros((self.nz - 2, 10))
+        tke = C.c_double()
+        self._check(self.L.nsmp_stats_plane(self.h, _p(out), C.byref(tke)))
+        return out, tke.value
 
     # ---- discrete adjoint ------------------------------------------------
     def _n0nz(self, a):

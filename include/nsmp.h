@@ -165,6 +165,30 @@ int nsmp_set_inner_solver(nsmp_ctx* ctx, double inner_tol, int inner_cap, int re
 /* Stream used by the context (cudaStream_t as void*). */
 void* nsmp_stream(nsmp_ctx* ctx);
 
+/* ---- turbulence statistics (Stats/stats.F90) ---------------------------- */
+
+/* Sums accumulated by nsmp_stats_sample, for nsmp_stats_download. */
+enum {
+    NSMP_S_U = 0, NSMP_S_V, NSMP_S_W, NSMP_S_P, NSMP_S_U2, NSMP_S_V2, NSMP_S_W2,
+    NSMP_S_UV, NSMP_S_VW, NSMP_S_WU, NSMP_S_P2, NSMP_S_EDDY, NSMP_NSTATS
+};
+/* sm_init (stats.F90:34-84): zero the sums and the sample count. */
+int nsmp_stats_reset(nsmp_ctx* ctx);
+/* glob_sample (stats.F90:91-197) on level n, to be called after
+ * nsmp_time_update where nsmp3D.F90:580-583 calls glob_sample(ufnp,...):
+ * adds u, v, w, p, their squares and cross products and nu_t (LES) of every
+ * interior cell and layer to the device sums. */
+int nsmp_stats_sample(nsmp_ctx* ctx);
+int nsmp_stats_count(nsmp_ctx* ctx, int* n);
+/* One sum as an (N_CELL,NZ) array (ghost rows zero), e.g. for SavetecStats. */
+int nsmp_stats_download(nsmp_ctx* ctx, int which, double* host);
+/* glob_put_plane_mm (stats.F90:204-384): for k = 2..NZ-1 a row of out
+ * ((NZ-2) rows x 10, row-major): yplus, mean u, v, w, rms u, v, w, and
+ * uv, vw, wu shear stresses (mean product minus product of means, as the
+ * reference writes them); *tke = the plane-averaged turbulent kinetic
+ * energy summed over layers / (NZ-2). */
+int nsmp_stats_plane(nsmp_ctx* ctx, double* out, double* tke);
+
 /* ---- discrete adjoint (an extension: the reference has none) ------------ */
 
 /* Body force on u per cell, (N0,NZ) column-major in the original cell

@@ -27,6 +27,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <array>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -58,6 +59,9 @@ enum { TagBCu = 1, TagBCv = 2, TagBCw = 3, TagBCp = 0 };
 
 struct orc_ctx {
     orc_params P;
+    // turbulence statistics (module_stats.F90): sm_uf .. sm_ef, sm_n
+    R2 sm[12];
+    int sm_n = 0;
     int has_fx = 0;
     R2 fx;               // body force on u, (N0,NZ) (extension)
     int N0, NV, NZ, NC;  // N_CELL0, N_VERT, NZ, N_CELL (= N_CELLexact)
@@ -1364,6 +1368,74 @@ int orc_step(orc_ctx* c, int fin_rk, orc_info* info) {
     c->ufn = c->ufnp; c->vfn = c->vfnp; c->wfn = c->wfnp; c->pfn = c->pfnp;
     if (info) { *info = c->info; info->iters = max_it; }
     return c->info.converged ? 0 : 1;
+}
+
+// sm_init (Stats/stats.F90:34-84)
+int orc_stats_reset(orc_ctx* c) {
+    for (int f = 0; f < 12; ++f) c->sm[f].init(c->NC, c->NZ, 0.0);
+    c->sm_n = 0;
+    return 0;
+}
+
+// glob_sample(ufn, vfn, wfn, pfn) after LoopTimeUpdate (Stats/stats.F90:137-180)
+int orc_stats_sample(orc_ctx* c) {
+    if (c->sm[0].d.empty()) orc_stats_reset(c);
+    for (int k = 1; k <= c->NZ; ++k)
+        for (int i = 1; i <= c->N0; ++i) {
+            const double tu = c->ufn(i, k), tv = c->vfn(i, k), tw = c->wfn(i, k), tp = c->pfn(i, k);
+            const double tp2 = tp * tp, tu2 = tu * tu, tv2 = tv * tv, tw2 = tw * tw;
+            const double tuv = tu * tv, tvw = tv * tw, twu = tw * tu;
+            c->sm[0](i, k) = c->sm[0](i, k) + tu;
+            c->sm[1](i, k) = c->sm[1](i, k) + tv;
+            c->sm[2](i, k) = c->sm[2](i, k) + tw;
+            c->sm[3](i, k) = c->sm[3](i, k) + tp;
+            c->sm[4](i, k) = c->sm[4](i, k) + tu2;
+            c->sm[5](i, k) = c->sm[5](i, k) + tv2;
+            c->sm[6](i, k) = c->sm[6](i, k) + tw2;
+            c->sm[7](i, k) = c->sm[7](i, k) + tuv;
+            c->sm[8](i, k) = c->sm[8](i, k) + tvw;
+            c->sm[9](i, k) = c->sm[9](i, k) + twu;
+            c->sm[10](i, k) = c->sm[10](i, k) + tp2;
+            if (c->P.les) c->sm[11](i, k) = c->sm[11](i, k) + c->eddy(i, k);
+        }
+    c->sm_n = c->sm_n + 1;
+    return 0;
+}
+
+int orc_stats_get(const orc_ctx* c, int which, double* out) {
+    if (which < 0 || which >= 12 || c->sm[which].d.empty()) return -1;
+    std::memcpy(out, c->sm[which].d.data(), c->sm[which].d.size() * sizeof(double));
+    return 0;
+}
+
+// glob_put_plane_mm (Stats/stats.F90:286-364): rows k = 2..NZ-1 of
+// yplus, u1m, v1m, w1m, urms, vrms, wrms, Tuvm, Tvwm, Twum; *tke.
+int orc_stats_plane(const orc_ctx* c, double* out, double* tke) {
+    const int NZ = c->NZ, ns = c->sm_n;
+    if (ns <= 0) return -1;
+    std::vector<std::array<double, 9>> S(NZ + 1);
+    for (auto& a : S) a.fill(0.0);
+    const int src[9] = {0, 1, 2, 4, 5, 6, 7, 8, 9};
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= c->N0; ++i)
+            for (int f = 0; f < 9; ++f) S[k][f] = S[k][f] + c->sm[src[f]](i, k) / ns;
+    const double npjx = 1.0 / c->N0;
+    double tkesum = 0.0;
+    for (int k = 2; k <= NZ - 1; ++k) {
+        const double yplus = c->P.re * (2 * k - 3) / (2 * NZ - 4);
+        const double u1m = S[k][0] * npjx, v1m = S[k][1] * npjx, w1m = S[k][2] * npjx;
+        const double u2m = S[k][3] * npjx, v2m = S[k][4] * npjx, w2m = S[k][5] * npjx;
+        const double uvm = S[k][6] * npjx, vwm = S[k][7] * npjx, wum = S[k][8] * npjx;
+        const double Tuvm = u1m * v1m - uvm, Tvwm = v1m * w1m - vwm, Twum = w1m * u1m - wum;
+        const double xrms = u2m - u1m * u1m, yrms = v2m - v1m * v1m, zrms = w2m - w1m * w1m;
+        tkesum = tkesum + 0.5 * (xrms + yrms + zrms);
+        double* o = out + (size_t)(k - 2) * 10;
+        o[0] = yplus; o[1] = u1m; o[2] = v1m; o[3] = w1m;
+        o[4] = std::sqrt(xrms); o[5] = std::sqrt(yrms); o[6] = std::sqrt(zrms);
+        o[7] = Tuvm; o[8] = Tvwm; o[9] = Twum;
+    }
+    *tke = tkesum / (NZ - 2);
+    return 0;
 }
 
 // Body force on u, (N0,NZ) column-major; NULL removes it.

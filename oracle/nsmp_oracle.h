@@ -100,6 +100,10 @@ int orc_step(orc_ctx* c, int fin_rk, orc_info* info);
 
 /* Operator hooks for unit parity tests. */
 int orc_set_body_force(orc_ctx* c, const double* fx);      /* (N0,NZ), NULL: none */
+int orc_stats_reset(orc_ctx* c);                           /* sm_init              */
+int orc_stats_sample(orc_ctx* c);                          /* glob_sample on level n */
+int orc_stats_get(const orc_ctx* c, int which, double* out);  /* (N_CELL,NZ)       */
+int orc_stats_plane(const orc_ctx* c, double* out, double* tke); /* (NZ-2) x 10    */
 int orc_apply_A(orc_ctx* c, const double* x, double* y);   /* (N_CELL,NZ) -> (N0..)*/
 int orc_gradient_lsm(orc_ctx* c, const double* f, double* dfdx, double* dfdy,
                      double* dfds);                         /* (N_CELL,NZ) each   */

@@ -66,6 +66,10 @@ def lib():
         L.orc_step.argtypes = [C.c_void_p, C.c_int, P(OrcInfo)]
         L.orc_apply_A.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_set_body_force.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_stats_reset.argtypes = [C.c_void_p]
+        L.orc_stats_sample.argtypes = [C.c_void_p]
+        L.orc_stats_get.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.orc_stats_plane.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_gradient_lsm.argtypes = [C.c_void_p] + [C.c_void_p] * 4
         L.orc_vertex_interp.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
         L.orc_mass_diag.argtypes = [C.c_void_p, C.c_void_p]
@@ -156,6 +160,23 @@ class Oracle:
     @flag_ab.setter
     def flag_ab(self, f):
         lib().orc_set_flag_ab(self.h, int(f))
+
+    def stats_reset(self):
+        lib().orc_stats_reset(self.h)
+
+    def stats_sample(self):
+        lib().orc_stats_sample(self.h)
+
+    def stats_get(self, which):
+        out = np.zeros((self.ncell, self.nz), order="F")
+        assert lib().orc_stats_get(self.h, int(which), _ptr(out)) == 0
+        return out
+
+    def stats_plane(self):
+        out = np.zeros((self.nz - 2, 10))
+        tke = C.c_double()
+        assert lib().orc_stats_plane(self.h, _ptr(out), C.byref(tke)) == 0
+        return out, tke.value
 
     def set_body_force(self, fx):
         if fx is None:
