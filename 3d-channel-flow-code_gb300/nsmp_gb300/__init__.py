@@ -64,7 +64,7 @@ EXPORTS = [
     "nsmp_set_inner_solver", "nsmp_solver_log", "nsmp_mass_diag_noalloc",
     "nsmp_set_body_force", "nsmp_wall_shear", "nsmp_adjoint", "nsmp_apply_A", "nsmp_apply_AT",
     "nsmp_set_adjoint_budget", "nsmp_stats_reset", "nsmp_stats_sample", "nsmp_stats_count",
-    "nsmp_stats_download", "nsmp_stats_plane",
+    "nsmp_stats_download", "nsmp_stats_plane", "nsmp_download_vertex",
 ]
 
 (K_VERTEX4, K_STAGE_RHS, K_FACES_DIV, K_BICG_INIT, K_BICG_P, K_BICG_SPMV_V, K_BICG_S, K_BICG_SPMV_T,
@@ -117,6 +117,7 @@ def lib(build_if_missing=True):
     L.nsmp_adjoint.argtypes = [vp, C.c_int, C.c_int, vp, vp, P(C.c_double)]
     L.nsmp_apply_A.argtypes = [vp, vp, vp]
     L.nsmp_set_adjoint_budget.argtypes = [vp, C.c_double]
+    L.nsmp_download_vertex.argtypes = [vp, C.c_int, C.c_int, vp]
     L.nsmp_stats_reset.argtypes = [vp]
     L.nsmp_stats_sample.argtypes = [vp]
     L.nsmp_stats_count.argtypes = [vp, P(C.c_int)]
@@ -307,6 +308,12 @@ class Solver:
     def mass_diag(self):
         out = np.zeros(4, dtype=np.float64)
         self._check(self.L.nsmp_mass_diag(self.h, _p(out)))
+        return out
+
+    def download_vertex(self, field, tagdir=3):
+        """Vertex values (N_VERT, NZ-1) of a level-n field (F_U .. F_P)."""
+        out = np.zeros((self.nvert, self.nz - 1), order="F")
+        self._check(self.L.nsmp_download_vertex(self.h, int(field), int(tagdir), _p(out)))
         return out
 
     # ---- turbulence statistics -------------------------------------------

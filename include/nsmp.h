@@ -165,6 +165,15 @@ int nsmp_set_inner_solver(nsmp_ctx* ctx, double inner_tol, int inner_cap, int re
 /* Stream used by the context (cudaStream_t as void*). */
 void* nsmp_stream(nsmp_ctx* ctx);
 
+/* ---- output path (Save/*.F90) ------------------------------------------- */
+
+/* Vertex values of a level-n field (NSMP_F_U .. NSMP_F_P) in the reference's
+ * vertex numbering, (N_VERT,NZ-1): tagdir 2 = the cell-layer vertex values
+ * of interpolation2D, tagdir 3 = blended to the vertex layers sigv(k) with
+ * the wall values of BCvelvertex3D (interpolation3D.F90:151-220,
+ * BC.F90:603-807, periodic copies averaged as bc_periodic does). */
+int nsmp_download_vertex(nsmp_ctx* ctx, int field, int tagdir, double* host);
+
 /* ---- turbulence statistics (Stats/stats.F90) ---------------------------- */
 
 /* Sums accumulated by nsmp_stats_sample, for nsmp_stats_download. */
