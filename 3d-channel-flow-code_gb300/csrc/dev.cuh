@@ -42,7 +42,6 @@ struct Scal {
     int pending;           // 1: FP64 update requested
     int restart;           // 1: restart the Krylov process at the next update
     int perturb;           // 1: perturb the shadow residual at that restart
-    int stall;             // 1: a bulk copy wait ran out (the solve stops with an error)
     int has_e;             // 1: e holds a correction
     int einc;              // 1: e lacks D^-1 (alpha p + omega s) of the last iteration
     int rfresh;            // 1: r was set by an FP64 update (else r = s - omega t)

@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kBlock) k_mix_init(Mesh m, MixArgs a, RedScrat
         sc->iiter = 0; sc->ksince = 0; sc->pending = 1; sc->restart = 1; sc->cur = 0;
         sc->has_e = 0; sc->einc = 0; sc->rfresh = 1;
         sc->iscale = 0.0;  // set from the first residual
-        sc->r2sq = 0.0; sc->rsum = 0.0; sc->theta = 1.0; sc->perturb = 0; sc->stall = 0;
+        sc->r2sq = 0.0; sc->rsum = 0.0; sc->theta = 1.0; sc->perturb = 0;
     }
 }
 
@@ -278,32 +278,6 @@ __global__ void __launch_bounds__(kBlock) k_in_pv(Mesh m, MixArgs a, RedScratch 
     }
 }
 
-// Last block of pass 2: omega, the next rho, the mean of e after this
-// iteration and the iteration-count tests, from the five reduced dots.
-__device__ __forceinline__ void st_finish(const Mesh& m, Scal* sc, const double (&tot)[5]) {
-    const double ts = tot[0], tt = tot[1];
-    if (!(tt > 0.0)) {  // t = 0 or not finite: restart from the FP64 truth
-        sc->pending = 1; sc->restart = 1; sc->einc = 0;
-        if (!(tt == tt)) sc->has_e = 0;
-        return;
-    }
-    const double om = ts / tt;
-    sc->iomega = om;
-    sc->emean = (sc->ise + sc->ialpha * sc->isy + om * tot[4]) / (double)m.nprism;
-    sc->irho_prev = sc->irho;
-    sc->irho = tot[2] - om * tot[3];  // (r0, s - omega t)
-    sc->iiter += 1;
-    sc->ksince += 1;
-    sc->iter += 1;
-    sc->has_e = 1;
-    sc->einc = 1;
-    if (!(om == om)) { sc->pending = 1; sc->restart = 1; sc->has_e = 0; sc->einc = 0; }
-    else if (sc->ksince >= sc->inner_cap) sc->pending = 1;
-    if (sc->pending && sc->iiter >= sc->restart_every) sc->restart = 1;
-    else if (sc->iter > sc->max_iters) sc->pending = 1;
-    else if (fabs(sc->irho_prev) < 1.0e-30 || fabs(om) < 1.0e-30) { sc->pending = 1; sc->restart = 1; }
-}
-
 // Pass 2: s = r - alpha v at the stencil points, t = A D^-1 s, the dots
 // (t, s), (t, t), (r0, s), (r0, t) and sum D^-1 s; then omega, the next rho,
 // the mean of e after this iteration and the iteration-count tests.  The
@@ -369,151 +343,28 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
         }
     }
     double tot[5];
-    if (grid_reduce_f<5>(f, rs, tot) && threadIdx.x == 0) st_finish(m, sc, tot);
-}
-
-// ---------------------------------------------------------------------------
-// Pass 2 with the column data staged in shared memory.  A block walks tiles
-// of kBlock x 4 consecutive prisms (one layer group per thread); r, v and
-// D^-1 of the next tile arrive by cp.async.bulk while the current tile
-// computes, completing on an mbarrier per buffer, so the contiguous streams
-// are in flight independently of occupancy.  Lateral neighbours are read
-// from global memory as in k_in_st.  Every wait is bounded: a copy that does
-// not complete sets sc->stall and ends the solve with an error instead of
-// hanging.
-// ---------------------------------------------------------------------------
-constexpr int kTileP = kBlock * 4;        // prisms per tile
-constexpr int kWaitCap = 1 << 22;         // try_wait polls before giving up
-
-__device__ __forceinline__ unsigned smem_u32(const void* p) {
-    return (unsigned)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-// true when the phase with the given parity has completed, within kWaitCap polls
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
-    for (int i = 0; i < kWaitCap; ++i) {
-        unsigned ok;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(ok)
-            : "r"(smem_u32(bar)), "r"(parity)
-            : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
-
-__global__ void __launch_bounds__(kBlock) k_in_st_tile(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
-    if (sc->done || sc->pending) return;
-    __shared__ __align__(128) float buf[2][3][kTileP];  // r, v, D^-1 of a tile
-    __shared__ __align__(8) unsigned long long bar[2];
-    __shared__ int stalled;
-    const int it = sc->iiter, nz = m.NZ, NZI = m.NZI;
-    const float al = (float)sc->ialpha;
-    const float* v = (it & 1) ? a.v0 : a.v1;
-    const int ntile = (m.nprism + kTileP - 1) / kTileP;
-    const int tid = threadIdx.x;
-    if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        stalled = 0;
-    }
-    __syncthreads();
-    auto issue = [&](int t, int b) {  // thread 0: copies of tile t into buffer b
-        const int cnt = min(kTileP, m.nprism - t * kTileP);
-        const unsigned bytes = (unsigned)cnt * sizeof(float);
-        const size_t g0 = (size_t)t * kTileP;
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(&bar[b], 3 * bytes);
-        bulk_g2s(buf[b][0], a.r + g0, bytes, &bar[b]);
-        bulk_g2s(buf[b][1], v + g0, bytes, &bar[b]);
-        bulk_g2s(buf[b][2], a.invD + g0, bytes, &bar[b]);
-    };
-    float f[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    auto zv = [&](size_t i) {
-        const FV<4> rr = ldv<4>(a.r, i), vv = ldv<4>(v, i), dd = ldv<4>(a.invD, i);
-        FV<4> z;
-#pragma unroll
-        for (int l = 0; l < 4; ++l) z[l] = fmaf(-al, vv[l], rr[l]) * dd[l];
-        return z;
-    };
-    auto z1 = [&](size_t i) { return fmaf(-al, v[i], a.r[i]) * a.invD[i]; };
-    int issued = 0, waited = 0;  // thread 0: tiles issued / completed waits
-    if (tid == 0 && (int)blockIdx.x < ntile) { issue(blockIdx.x, 0); issued = 1; }
-    for (int t = blockIdx.x, i = 0; t < ntile; t += gridDim.x, ++i) {
-        const int b = i & 1;
-        const int tn = t + gridDim.x;
-        if (tn < ntile && tid == 0) { issue(tn, b ^ 1); ++issued; }
-        if (mbar_wait(&bar[b], (unsigned)((i >> 1) & 1))) {
-            if (tid == 0) ++waited;
-        } else {
-            stalled = 1;
-        }
-        __syncthreads();
-        if (stalled) break;
-        const int cnt = min(kTileP, m.nprism - t * kTileP);
-        const int lo = tid * 4;
-        if (lo < cnt) {
-            const int g = t * kTileP + lo;
-            const int c = g / NZI, kk = g - c * NZI;
-            const int k0 = kk + 1;
-            const ColPPE32& P = a.ppe32[c];
-            FV<4> s0, z0;
-#pragma unroll
-            for (int l = 0; l < 4; ++l) {
-                s0[l] = fmaf(-al, buf[b][1][lo + l], buf[b][0][lo + l]);
-                z0[l] = s0[l] * buf[b][2][lo + l];
-            }
-            float zT = 0.f, zB = 0.f;
-            if (kk + 4 < NZI)
-                zT = (lo + 4 < cnt) ? fmaf(-al, buf[b][1][lo + 4], buf[b][0][lo + 4]) * buf[b][2][lo + 4] : z1(g + 4);
-            if (kk > 0)
-                zB = (lo > 0) ? fmaf(-al, buf[b][1][lo - 1], buf[b][0][lo - 1]) * buf[b][2][lo - 1] : z1(g - 1);
-            const FV<4> n1 = zv(g + (size_t)(P.nb[0] - c) * NZI);
-            const FV<4> n2 = zv(g + (size_t)(P.nb[1] - c) * NZI);
-            const FV<4> n3 = zv(g + (size_t)(P.nb[2] - c) * NZI);
-            FV<4> tt;
-#pragma unroll
-            for (int l = 0; l < 4; ++l)
-                tt[l] = a_row32(a, nz, P, k0 + l, z0[l], n1[l], n2[l], n3[l], (l + 1 < 4) ? z0[l + 1] : zT,
-                                (l > 0) ? z0[l - 1] : zB);
-            stv<4>(a.s, g, s0);
-            stv<4>(a.t, g, tt);
-            const FV<4> q0 = ldv<4>(a.r0, g);
-#pragma unroll
-            for (int l = 0; l < 4; ++l) {
-                f[0] = fmaf(tt[l], s0[l], f[0]);
-                f[1] = fmaf(tt[l], tt[l], f[1]);
-                f[2] = fmaf(q0[l], s0[l], f[2]);
-                f[3] = fmaf(q0[l], tt[l], f[3]);
-                f[4] += z0[l];
-            }
-        }
-        __syncthreads();  // buffer b is refilled two tiles later
-    }
-    if (stalled && tid == 0) {
-        // let the copies still in flight land before the block's shared
-        // memory goes away (bounded as well), then report
-        for (int j = waited; j < issued; ++j) mbar_wait(&bar[j & 1], (unsigned)((j >> 1) & 1));
-        sc->stall = 1;
-    }
-    double tot[5];
     if (grid_reduce_f<5>(f, rs, tot) && threadIdx.x == 0) {
-        if (sc->stall) { sc->done = 1; sc->status = NSMP_ERR_CUDA; return; }
-        st_finish(m, sc, tot);
+        const double ts = tot[0], tt = tot[1];
+        if (!(tt > 0.0)) {  // t = 0 or not finite: restart from the FP64 truth
+            sc->pending = 1; sc->restart = 1; sc->einc = 0;
+            if (!(tt == tt)) sc->has_e = 0;
+            return;
+        }
+        const double om = ts / tt;
+        sc->iomega = om;
+        sc->emean = (sc->ise + sc->ialpha * sc->isy + om * tot[4]) / (double)m.nprism;
+        sc->irho_prev = sc->irho;
+        sc->irho = tot[2] - om * tot[3];  // (r0, s - omega t)
+        sc->iiter += 1;
+        sc->ksince += 1;
+        sc->iter += 1;
+        sc->has_e = 1;
+        sc->einc = 1;
+        if (!(om == om)) { sc->pending = 1; sc->restart = 1; sc->has_e = 0; sc->einc = 0; }
+        else if (sc->ksince >= sc->inner_cap) sc->pending = 1;
+        if (sc->pending && sc->iiter >= sc->restart_every) sc->restart = 1;
+        else if (sc->iter > sc->max_iters) sc->pending = 1;
+        else if (fabs(sc->irho_prev) < 1.0e-30 || fabs(om) < 1.0e-30) { sc->pending = 1; sc->restart = 1; }
     }
 }
 
@@ -786,8 +637,6 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     const int L = quad ? 4 : 2;
     const int g_pv = quad ? grid_occ(c, k_in_pv<4>, m.nprism / L) : grid_occ(c, k_in_pv<2>, m.nprism / L);
     const int g_st = quad ? grid_occ(c, k_in_st<4>, m.nprism / L) : grid_occ(c, k_in_st<2>, m.nprism / L);
-    const int g_tl = quad ? std::min(grid_occ(c, k_in_st_tile, m.nprism / L), (m.nprism + kTileP - 1) / kTileP) : 1;
-    (void)g_tl;
     const int g_in = grid_occ(c, k_mix_init, m.nprism), g_u = grid_occ(c, k_mix_update, m.nprism);
     const int g_sc = grid_occ(c, k_mix_scale, m.nprism), g_sh = grid_occ(c, k_mix_shadow, m.nprism);
     MixArgs a{c->rhsp, pf, c->b64, c->r, c->x, c->xa, c->xb, c->r32, c->r032, c->p32[0], c->p32[1], c->v32[0],
@@ -826,10 +675,6 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
         CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         prof_resolve(c);
-        if (c->h_scal->stall) {
-            c->err = "mixed solver: a bulk copy into shared memory did not complete within its wait limit";
-            return NSMP_ERR_CUDA;
-        }
         if (c->h_scal->done) break;
         if (launched > 4 * ((long long)c->prm.max_iters + 2000 * 8)) {
             c->err = "mixed solver did not stop";
