@@ -174,3 +174,29 @@ def test_adjoint_in_mixed_precision_agrees_with_fp64():
     assert abs(J32 - J64) <= 1e-9 * abs(J64)
     assert np.linalg.norm(g32 - g64) <= 1e-6 * np.linalg.norm(g64)
     s.close()
+
+
+def test_autograd_function_matches_the_adjoint():
+    """J.backward() through the torch.autograd.Function fills fx.grad with
+    the adjoint gradient, and the Function's J matches a finite difference."""
+    import torch
+    from nsmp_gb300.autograd import capture_state, wall_shear_objective
+    prm, mesh, s = _solver()
+    n0, nz = prm["n0"], prm["nz"]
+    st = capture_state(s)
+    f0 = _interior_random(np.random.default_rng(2), n0, nz, 0.01)
+    fx = torch.tensor(f0, dtype=torch.float64, requires_grad=True)
+    J = wall_shear_objective(s, fx, st, 3, 2)
+    J.backward()
+    s.upload_state(*st[0], st[1], st[2], 0)
+    _, g_ref, rc = s.adjoint(3, 2, f0)
+    assert rc == 0
+    assert np.linalg.norm(fx.grad.numpy() - g_ref) <= 1e-6 * np.linalg.norm(g_ref)
+    d = _interior_random(np.random.default_rng(7), n0, nz)
+    h = 1e-4
+    with torch.no_grad():
+        Jp = wall_shear_objective(s, torch.tensor(f0 + h * d), st, 3, 2).item()
+        Jm = wall_shear_objective(s, torch.tensor(f0 - h * d), st, 3, 2).item()
+    fd = (Jp - Jm) / (2 * h)
+    assert abs(fd - float(np.sum(fx.grad.numpy() * d))) <= 1e-5 * abs(fd)
+    s.close()
