@@ -12,7 +12,7 @@ constexpr int kMaxRed = 8;    // values reduced at once
 // Per-layer factor rows of the level table (lev[row*NZ + k0]).
 enum LevRow {
     LV_DSV = 0, LV_IDSV, LV_IDST, LV_IDSB, LV_IDSBU, LV_WT, LV_WB, LV_GZP, LV_GZM, LV_HMEAN,
-    LV_DD, LV_KD, LV_DAMP, LV_IHZ, LV_COUNT
+    LV_DD, LV_KD, LV_DAMP, LV_IHZ, LV_ATOP, LV_ABOT, LV_COUNT
 };
 
 // Scalars of one stage kept in device memory between kernels.
@@ -42,6 +42,7 @@ struct Scal {
     int pending;           // 1: FP64 update requested
     int restart;           // 1: restart the Krylov process at the next update
     int perturb;           // 1: perturb the shadow residual at that restart
+    int verify;            // 1: the next FP64 update recomputes b - A x to confirm convergence
     int has_e;             // 1: e holds a correction
     int einc;              // 1: e lacks D^-1 (alpha p + omega s) of the last iteration
     int rfresh;            // 1: r was set by an FP64 update (else r = s - omega t)

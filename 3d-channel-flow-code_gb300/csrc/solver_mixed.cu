@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kBlock) k_mix_init(Mesh m, MixArgs a, RedScrat
         sc->iiter = 0; sc->ksince = 0; sc->pending = 1; sc->restart = 1; sc->cur = 0;
         sc->has_e = 0; sc->einc = 0; sc->rfresh = 1;
         sc->iscale = 0.0;  // set from the first residual
-        sc->r2sq = 0.0; sc->rsum = 0.0; sc->theta = 1.0; sc->perturb = 0;
+        sc->r2sq = 0.0; sc->rsum = 0.0; sc->theta = 1.0; sc->perturb = 0; sc->verify = 0;
     }
 }
 
@@ -382,6 +382,7 @@ __global__ void __launch_bounds__(kBlock) k_mix_update(Mesh m, MixArgs a, RedScr
     const int cur = sc->cur;
     const int has_e = sc->has_e;
     const int first = (sc->iscale == 0.0);
+    const int full = first || sc->verify;
     const int einc = has_e && sc->einc;
     const double scale = sc->iscale;
     const float em = (float)sc->emean;
@@ -397,18 +398,35 @@ __global__ void __launch_bounds__(kBlock) k_mix_update(Mesh m, MixArgs a, RedScr
         prism_of(m, g, c, k0);
         const ColPPE& P = m.ppe[c];
         const size_t q = g;
-        auto xn = [&](size_t i) {
-            if (!has_e) return xin[i];
-            float e = a.e[i];
-            if (einc) e = fmaf(a.invD[i], fmaf(om, a.s[i], al * pl[i]), e);
-            return fma(scale, (double)(e - em), xin[i]);
-        };
-        const double x0 = xn(q);
-        const double xT = (k0 < m.NZ - 2) ? xn(q + 1) : 0.0;
-        const double xB = (k0 > 1) ? xn(q - 1) : 0.0;
-        const double Ax = ppe_row(m, P, k0, x0, xn(ICg(m, P.nb[0], k0)), xn(ICg(m, P.nb[1], k0)),
-                                  xn(ICg(m, P.nb[2], k0)), xT, xB);
-        const double r = a.b[q] - Ax;
+        double x0, r;
+        if (full) {  // b - A x from scratch: the initial residual, or the check of a converged one
+            x0 = xin[q];
+            const double xT = (k0 < m.NZ - 2) ? xin[q + 1] : 0.0;
+            const double xB = (k0 > 1) ? xin[q - 1] : 0.0;
+            r = a.b[q] - ppe_row(m, P, k0, x0, xin[ICg(m, P.nb[0], k0)], xin[ICg(m, P.nb[1], k0)],
+                                 xin[ICg(m, P.nb[2], k0)], xT, xB);
+        } else if (!has_e) {
+            x0 = xin[q];
+            r = rin[q];
+        } else {
+            // x1 = x + iscale c with c = e - mean e exactly as stored, and
+            // r1 = r - iscale A c in FP64 from the differences of c (A 1 = 0):
+            // the residual of the stored x1, at ~25 FP64 instructions a prism
+            auto cv = [&](size_t i) {
+                float e = a.e[i];
+                if (einc) e = fmaf(a.invD[i], fmaf(om, a.s[i], al * pl[i]), e);
+                return (double)(e - em);
+            };
+            const double c0 = cv(q);
+            const double dT = (k0 < m.NZ - 2) ? cv(q + 1) - c0 : 0.0;
+            const double dB = (k0 > 1) ? cv(q - 1) - c0 : 0.0;
+            const double d1 = cv(ICg(m, P.nb[0], k0)) - c0, d2 = cv(ICg(m, P.nb[1], k0)) - c0,
+                         d3 = cv(ICg(m, P.nb[2], k0)) - c0;
+            const double Ac = lev(m, LV_DSV, k0) * (P.kA[0] * d1 + P.kA[1] * d2 + P.kA[2] * d3) +
+                              P.area * (lev(m, LV_ATOP, k0) * dT + lev(m, LV_ABOT, k0) * dB);
+            x0 = fma(scale, c0, xin[q]);
+            r = fma(-scale, Ac, rin[q]);
+        }
         xout[q] = x0;
         rout[q] = r;
         part[0] += r * r;
@@ -466,7 +484,11 @@ __global__ void __launch_bounds__(kBlock) k_mix_scale(Mesh m, MixArgs a, RedScra
     const double* ro = cur ? a.r64b : a.r64a;
     double* xn = cur ? a.xa : a.xb;
     double* rn = cur ? a.r64a : a.r64b;
-    double part[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    // the FP64 residual's norms for the stopping test and the next update are
+    // taken from its FP32 image r = iscale (rf + rm / iscale), to FP32
+    // accuracy, so the pass costs three FP64 instructions a prism
+    const float rmi = (float)(rm * inv);
+    float part[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
         double r = rn[g];
         if (blend) {
@@ -474,40 +496,46 @@ __global__ void __launch_bounds__(kBlock) k_mix_scale(Mesh m, MixArgs a, RedScra
             rn[g] = r;
             xn[g] = fma(th, xn[g] - xo[g], xo[g]);
         }
-        part[0] += fabs(r);
-        part[1] += r * r;
-        part[2] += r;
         const float rf = (float)((r - rm) * inv);
         a.r[g] = rf;
         a.e[g] = 0.f;
-        const double rd = (double)rf;
-        part[3] += fabs(rd);
-        part[4] += rd * rd;
+        const float ra = rf + rmi;
+        part[0] += fabsf(ra);
+        part[1] = fmaf(ra, ra, part[1]);
+        part[2] += ra;
+        part[3] += fabsf(rf);
+        part[4] = fmaf(rf, rf, part[4]);
     }
     double tot[5];
-    if (grid_reduce<5, false>(part, rs, tot) && threadIdx.x == 0) {
-        const double r1 = tot[0], r2 = sqrt(tot[1]);
+    if (grid_reduce_f<5>(part, rs, tot) && threadIdx.x == 0) {
+        const double is = sc->iscale;
+        const double r1 = is * tot[0], r2 = is * sqrt(tot[1]);
         const int k = (sc->outer - 1) % Scal::kCycLog;
         sc->cyc_out[k] = (float)(r2 / sc->b2);
         sc->cur = cur ^ 1;
         sc->r1 = r1; sc->r2 = r2;
-        sc->r2sq = tot[1];
-        sc->rsum = tot[2];
+        sc->r2sq = is * is * tot[1];
+        sc->rsum = is * tot[2];
         sc->e1 = r1 / sc->b1; sc->e2 = r2 / sc->b2;
         sc->cyc_acc[k] = (th == 1.0 ? 1 : 0) | (sc->restart ? 2 : 0);
         sc->ib1 = (tot[3] > 0.0) ? tot[3] : 1.0;
         sc->ib2 = (tot[4] > 0.0) ? sqrt(tot[4]) : 1.0;
         const double en = fmin(sc->e1, sc->e2);
+        // the incremental residual drifts from b - A x by FP64 rounding over
+        // the updates: when it passes the test, the next update recomputes
+        // b - A x from scratch and the test is taken again on that
         if (!(r2 == r2)) { sc->status = NSMP_ERR_NAN; sc->done = 1; }
-        else if (en < sc->eps) { sc->converged = 1; sc->done = 1; }
+        else if (en < sc->eps && sc->verify) { sc->converged = 1; sc->done = 1; }
+        else if (en < sc->eps) { sc->verify = 1; }
         else if (sc->iter > sc->max_iters) { sc->status = NSMP_WARN_MAXITER; sc->done = 1; }
         else if (sc->outer >= 2000) { sc->status = NSMP_WARN_BREAKDOWN; sc->done = 1; }
+        if (!(en < sc->eps)) sc->verify = 0;
     }
 }
 
 // Shadow residual and rho for the next FP32 cycle (after k_mix_scale).
 __global__ void __launch_bounds__(kBlock) k_mix_shadow(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
-    if (sc->done || !sc->pending) return;
+    if (sc->done || !sc->pending || sc->verify) return;  // a check of b - A x is pending
     const int rst = sc->restart, jit = sc->perturb;
     const unsigned int salt = (unsigned int)sc->outer;
     double part[1] = {0.0};

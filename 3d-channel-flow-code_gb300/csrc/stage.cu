@@ -681,11 +681,16 @@ int ctx_init_device(nsmp_ctx* c) {
     std::vector<double> lv((size_t)LV_COUNT * L.NZ, 0.0);
     const Levels& V = L.lev;
     const std::vector<double>* rows[LV_COUNT] = {&V.dsv, nullptr, &V.idsT, &V.idsB, &V.idsBu, &V.wT, &V.wB,
-                                                 &V.gzp, &V.gzm, &V.hmean, &V.les_dd, &V.les_kd, &V.les_damp, &V.ihz};
+                                                 &V.gzp, &V.gzm, &V.hmean, &V.les_dd, &V.les_kd, &V.les_damp, &V.ihz,
+                                                 nullptr, nullptr};
     for (int r = 0; r < LV_COUNT; ++r)
         for (int k = 0; k < L.NZ; ++k) {
-            if (r == LV_IDSV) lv[(size_t)r * L.NZ + k] = (V.dsv[k] != 0.0) ? 1.0 / V.dsv[k] : 0.0;
-            else lv[(size_t)r * L.NZ + k] = (*rows[r])[k];
+            double val;
+            if (r == LV_IDSV) val = (V.dsv[k] != 0.0) ? 1.0 / V.dsv[k] : 0.0;
+            else if (r == LV_ATOP) val = V.idsT[k] * V.wT[k];  // PPE coupling / area to the layer above
+            else if (r == LV_ABOT) val = V.idsB[k] * V.wB[k];  // and below (0 at the walls)
+            else val = (*rows[r])[k];
+            lv[(size_t)r * L.NZ + k] = val;
         }
     CK(cudaMemcpyAsync(c->d_lev, lv.data(), sizeof(double) * lv.size(), cudaMemcpyHostToDevice, c->stream));
     std::vector<int> gcol(L.NC), vg(L.NV);
