@@ -129,9 +129,15 @@ __device__ __forceinline__ void stv(float* p, size_t i, const FV<L>& o) {
 //   0: first iteration of a Krylov process:  p = r
 //   1: first iteration after an FP64 update: p = r + beta (p - omega v), r stored
 //   2: otherwise:                            r = s - omega t, p = r + beta (p - omega v)
+// The FP32 Krylov vectors are stored scaled by D^-1 (r~ = D^-1 r, p~, v~,
+// s~, t~; the shadow residual as r^0 = D r0): a change of variables that
+// leaves the right-preconditioned iteration unchanged in exact arithmetic,
+// while the operator's input D^-1 p is then p~ itself, so a stencil point
+// needs no D^-1 load.  D^-1 is read only at the centre, where v~ = D^-1 A p~
+// is formed and the unscaled values the dots need are recovered.
 template <int MODE>
 __device__ __forceinline__ float pv_p1(const MixArgs& a, const float* pin, const float* vin, float beta, float om,
-                                       size_t i) {
+                                       size_t i) {  // p~ at one point
     if (MODE == 0) return a.r[i];
     const float r = (MODE == 1) ? a.r[i] : fmaf(-om, a.t[i], a.s[i]);
     return fmaf(beta, fmaf(-om, vin[i], pin[i]), r);
@@ -139,8 +145,7 @@ __device__ __forceinline__ float pv_p1(const MixArgs& a, const float* pin, const
 
 template <int MODE, int L>
 __device__ __forceinline__ FV<L> pv_yv(const MixArgs& a, const float* pin, const float* vin, float beta, float om,
-                                       size_t i) {  // D^-1 p at layers i .. i+L-1
-    const FV<L> dd = ldv<L>(a.invD, i);
+                                       size_t i) {  // p~ = D^-1 p at layers i .. i+L-1
     FV<L> r, y;
     if (MODE == 2) {
         const FV<L> ss = ldv<L>(a.s, i), tt = ldv<L>(a.t, i);
@@ -149,14 +154,10 @@ __device__ __forceinline__ FV<L> pv_yv(const MixArgs& a, const float* pin, const
     } else {
         r = ldv<L>(a.r, i);
     }
-    if (MODE == 0) {
-#pragma unroll
-        for (int l = 0; l < L; ++l) y[l] = r[l] * dd[l];
-        return y;
-    }
+    if (MODE == 0) return r;
     const FV<L> pp = ldv<L>(pin, i), vv = ldv<L>(vin, i);
 #pragma unroll
-    for (int l = 0; l < L; ++l) y[l] = fmaf(beta, fmaf(-om, vv[l], pp[l]), r[l]) * dd[l];
+    for (int l = 0; l < L; ++l) y[l] = fmaf(beta, fmaf(-om, vv[l], pp[l]), r[l]);
     return y;
 }
 
@@ -191,10 +192,11 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
                 r[l] = fmaf(-om, tt[l], ss[l]);
                 p[l] = fmaf(beta, fmaf(-om, vv[l], pp[l]), r[l]);
                 // increment of the previous iteration: e += D^-1 (alpha p + omega s)
-                e[l] = fmaf(dd[l], fmaf(om, ss[l], al * pp[l]), e[l]);
+                e[l] = e[l] + fmaf(om, ss[l], al * pp[l]);
                 f[1] += e[l];
-                f[3] += fabsf(r[l]);
-                f[4] = fmaf(r[l], r[l], f[4]);
+                const float ru = r[l] * __frcp_rn(dd[l]);  // unscaled r
+                f[3] += fabsf(ru);
+                f[4] = fmaf(ru, ru, f[4]);
             }
             stv<L>(a.e, g, e);
             stv<L>(a.r, g, r);
@@ -210,31 +212,28 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
                 for (int l = 0; l < L; ++l) p[l] = fmaf(beta, fmaf(-om, vv[l], pp[l]), r[l]);
             }
         }
-        FV<L> y;
-#pragma unroll
-        for (int l = 0; l < L; ++l) y[l] = p[l] * dd[l];
-        float yT = __shfl_down_sync(0xffffffffu, y[0], 1);
-        float yB = __shfl_up_sync(0xffffffffu, y[L - 1], 1);
+        float yT = __shfl_down_sync(0xffffffffu, p[0], 1);
+        float yB = __shfl_up_sync(0xffffffffu, p[L - 1], 1);
         if (!act) continue;
         if (kk + L >= NZI) yT = 0.f;
-        else if (lane == 31 || h + 1 >= ngrp) yT = pv_p1<MODE>(a, pin, vin, beta, om, g + L) * a.invD[g + L];
+        else if (lane == 31 || h + 1 >= ngrp) yT = pv_p1<MODE>(a, pin, vin, beta, om, g + L);
         if (kk == 0) yB = 0.f;
-        else if (lane == 0) yB = pv_p1<MODE>(a, pin, vin, beta, om, g - 1) * a.invD[g - 1];
+        else if (lane == 0) yB = pv_p1<MODE>(a, pin, vin, beta, om, g - 1);
         const FV<L> n1 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[0] - c) * NZI);
         const FV<L> n2 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[1] - c) * NZI);
         const FV<L> n3 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[2] - c) * NZI);
         FV<L> v;
 #pragma unroll
         for (int l = 0; l < L; ++l)
-            v[l] = a_row32(a, nz, P, k0 + l, y[l], n1[l], n2[l], n3[l], (l + 1 < L) ? y[l + 1] : yT,
-                           (l > 0) ? y[l - 1] : yB);
+            v[l] = a_row32(a, nz, P, k0 + l, p[l], n1[l], n2[l], n3[l], (l + 1 < L) ? p[l + 1] : yT,
+                           (l > 0) ? p[l - 1] : yB) * dd[l];  // v~ = D^-1 A p~
         stv<L>(pout, g, p);
         stv<L>(vout, g, v);
         const FV<L> q0 = ldv<L>(a.r0, g);
 #pragma unroll
         for (int l = 0; l < L; ++l) {
-            f[0] = fmaf(q0[l], v[l], f[0]);
-            f[2] += y[l];
+            f[0] = fmaf(q0[l], v[l], f[0]);  // (r0, v) = (r^0, v~)
+            f[2] += p[l];
         }
     }
 }
@@ -292,14 +291,14 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
     const float* v = (it & 1) ? a.v0 : a.v1;
     const int ngrp = m.nprism / L;
     float f[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    auto zv = [&](size_t i) {
-        const FV<L> rr = ldv<L>(a.r, i), vv = ldv<L>(v, i), dd = ldv<L>(a.invD, i);
+    auto zv = [&](size_t i) {  // s~ = r~ - alpha v~ = D^-1 s
+        const FV<L> rr = ldv<L>(a.r, i), vv = ldv<L>(v, i);
         FV<L> z;
 #pragma unroll
-        for (int l = 0; l < L; ++l) z[l] = fmaf(-al, vv[l], rr[l]) * dd[l];
+        for (int l = 0; l < L; ++l) z[l] = fmaf(-al, vv[l], rr[l]);
         return z;
     };
-    auto z1 = [&](size_t i) { return fmaf(-al, v[i], a.r[i]) * a.invD[i]; };
+    auto z1 = [&](size_t i) { return fmaf(-al, v[i], a.r[i]); };
     const int lane = threadIdx.x & 31;
     for (int hw = blockIdx.x * blockDim.x + (threadIdx.x & ~31); hw < ngrp; hw += gridDim.x * blockDim.x) {
         const int h = hw + lane;
@@ -309,12 +308,9 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
         const int k0 = kk + 1;
         const ColPPE32& P = a.ppe32[c];
         const FV<L> rr = ldv<L>(a.r, g), vv = ldv<L>(v, g), dd = ldv<L>(a.invD, g);
-        FV<L> s0, z0;
+        FV<L> z0;
 #pragma unroll
-        for (int l = 0; l < L; ++l) {
-            s0[l] = fmaf(-al, vv[l], rr[l]);
-            z0[l] = s0[l] * dd[l];
-        }
+        for (int l = 0; l < L; ++l) z0[l] = fmaf(-al, vv[l], rr[l]);
         float zT = __shfl_down_sync(0xffffffffu, z0[0], 1);
         float zB = __shfl_up_sync(0xffffffffu, z0[L - 1], 1);
         if (!act) continue;
@@ -330,15 +326,19 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
         for (int l = 0; l < L; ++l)
             t[l] = a_row32(a, nz, P, k0 + l, z0[l], n1[l], n2[l], n3[l], (l + 1 < L) ? z0[l + 1] : zT,
                            (l > 0) ? z0[l - 1] : zB);
-        stv<L>(a.s, g, s0);
-        stv<L>(a.t, g, t);
+        FV<L> tt;
+#pragma unroll
+        for (int l = 0; l < L; ++l) tt[l] = t[l] * dd[l];
+        stv<L>(a.s, g, z0);
+        stv<L>(a.t, g, tt);
         const FV<L> q0 = ldv<L>(a.r0, g);
 #pragma unroll
         for (int l = 0; l < L; ++l) {
-            f[0] = fmaf(t[l], s0[l], f[0]);
-            f[1] = fmaf(t[l], t[l], f[1]);
-            f[2] = fmaf(q0[l], s0[l], f[2]);
-            f[3] = fmaf(q0[l], t[l], f[3]);
+            const float su = z0[l] * __frcp_rn(dd[l]);  // unscaled s
+            f[0] = fmaf(t[l], su, f[0]);       // (t, s)
+            f[1] = fmaf(t[l], t[l], f[1]);     // (t, t)
+            f[2] = fmaf(q0[l], z0[l], f[2]);   // (r0, s) = (r^0, s~)
+            f[3] = fmaf(q0[l], tt[l], f[3]);   // (r0, t) = (r^0, t~)
             f[4] += z0[l];
         }
     }
@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(kBlock) k_mix_update(Mesh m, MixArgs a, RedScr
             // the residual of the stored x1, at ~25 FP64 instructions a prism
             auto cv = [&](size_t i) {
                 float e = a.e[i];
-                if (einc) e = fmaf(a.invD[i], fmaf(om, a.s[i], al * pl[i]), e);
+                if (einc) e = e + fmaf(om, a.s[i], al * pl[i]);  // D^-1 (alpha p + omega s)
                 return (double)(e - em);
             };
             const double c0 = cv(q);
@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(kBlock) k_mix_scale(Mesh m, MixArgs a, RedScra
             xn[g] = fma(th, xn[g] - xo[g], xo[g]);
         }
         const float rf = (float)((r - rm) * inv);
-        a.r[g] = rf;
+        a.r[g] = rf * a.invD[g];  // r~ = D^-1 r
         a.e[g] = 0.f;
         const float ra = rf + rmi;
         part[0] += fabsf(ra);
@@ -540,15 +540,16 @@ __global__ void __launch_bounds__(kBlock) k_mix_shadow(Mesh m, MixArgs a, RedScr
     const unsigned int salt = (unsigned int)sc->outer;
     double part[1] = {0.0};
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
-        const float rf = a.r[g];
-        float q0;
+        const float rt = a.r[g];  // r~ = D^-1 r
         if (rst) {
-            q0 = jit ? rf * (1.0f + 0.5f * shadow_jitter((unsigned int)g, salt)) : rf;
-            a.r0[g] = q0;
+            const float d = __frcp_rn(a.invD[g]);
+            const float rf = rt * d;  // r
+            const float q0 = jit ? rf * (1.0f + 0.5f * shadow_jitter((unsigned int)g, salt)) : rf;
+            a.r0[g] = q0 * d;  // r^0 = D r0
+            part[0] += (double)q0 * (double)rf;
         } else {
-            q0 = a.r0[g];
+            part[0] += (double)a.r0[g] * (double)rt;  // (r0, r) = (r^0, r~)
         }
-        part[0] += (double)q0 * (double)rf;
     }
     double tot[1];
     if (grid_reduce<1, false>(part, rs, tot) && threadIdx.x == 0) {
