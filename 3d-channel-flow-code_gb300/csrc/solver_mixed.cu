@@ -49,17 +49,26 @@ struct MixArgs {
     float *r, *r0, *p0, *p1, *v0, *v1, *s, *t, *e;
     const float* invD;
     const ColPPE32* ppe32;
-    const float* lev32; // rows: dsigv(k-1), wT/dsig(k), wB/dsig(k-1)
+    const float4* lev32; // per level k0: {dsigv(k-1), wT/dsig(k), wB/dsig(k-1), 0}
 };
 
-__device__ __forceinline__ float lv32(const MixArgs& a, int nz, int row, int k0) { return __ldg(a.lev32 + row * nz + k0); }
+// The 32-byte column record as two 16-byte loads.
+__device__ __forceinline__ ColPPE32 ld_col(const ColPPE32* p) {
+    const int4 q0 = __ldg(reinterpret_cast<const int4*>(p));
+    const float4 q1 = __ldg(reinterpret_cast<const float4*>(p) + 1);
+    ColPPE32 P;
+    P.nb[0] = q0.x; P.nb[1] = q0.y; P.nb[2] = q0.z;
+    P.kA[0] = __int_as_float(q0.w); P.kA[1] = q1.x; P.kA[2] = q1.y;
+    P.area = q1.z; P.pad = q1.w;
+    return P;
+}
 
 // FP32 operator row: A y at one prism (same coefficients as ppe_row).
-__device__ __forceinline__ float a_row32(const MixArgs& a, int nz, const ColPPE32& P, int k0, float y0, float y1,
-                                         float y2, float y3, float yT, float yB) {
-    const float dsv = lv32(a, nz, 0, k0);
-    const float AA1 = P.kA[0] * dsv, AA2 = P.kA[1] * dsv, AA3 = P.kA[2] * dsv;
-    const float AAT = P.area * lv32(a, nz, 1, k0), AAB = P.area * lv32(a, nz, 2, k0);
+__device__ __forceinline__ float a_row32(const MixArgs& a, const ColPPE32& P, int k0, float y0, float y1, float y2,
+                                         float y3, float yT, float yB) {
+    const float4 q = __ldg(a.lev32 + k0);
+    const float AA1 = P.kA[0] * q.x, AA2 = P.kA[1] * q.x, AA3 = P.kA[2] * q.x;
+    const float AAT = P.area * q.y, AAB = P.area * q.z;
     const float AA0 = -(AAT + AAB + AA1 + AA2 + AA3);
     return AA0 * y0 + AA1 * y1 + AA2 * y2 + AA3 * y3 + AAT * yT + AAB * yB;
 }
@@ -166,7 +175,7 @@ __device__ __forceinline__ FV<L> pv_yv(const MixArgs& a, const float* pin, const
 template <int MODE, int L>
 __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it, float beta, float om, float al,
                                          float (&f)[5]) {
-    const int nz = m.NZ, NZI = m.NZI;
+    const int NZI = m.NZI;
     const float* pin = (it & 1) ? a.p1 : a.p0;
     const float* vin = (it & 1) ? a.v1 : a.v0;
     float* pout = (it & 1) ? a.p0 : a.p1;
@@ -174,35 +183,34 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
     const int ngrp = m.nprism / L;
     const int lane = threadIdx.x & 31;
     // warp-uniform trip count: the vertical neighbours of a group are the
-    // end layers of the adjacent lanes' groups (shuffled, not reloaded)
+    // end layers of the adjacent lanes' groups (shuffled, not reloaded).
+    // Every load of a group (centre, column ends, lateral neighbours, r^0)
+    // is issued before the shuffle and before any store of the group, so all
+    // are in flight together; lanes past the end repeat the warp's first
+    // group and store nothing.
     for (int hw = blockIdx.x * blockDim.x + (threadIdx.x & ~31); hw < ngrp; hw += gridDim.x * blockDim.x) {
         const int h = hw + lane;
         const bool act = h < ngrp;
         const int g = L * (act ? h : hw);
         const int c = g / NZI, kk = g - c * NZI;  // layers k0 = kk+1 .. kk+L
         const int k0 = kk + 1;
-        const ColPPE32& P = a.ppe32[c];
-        const FV<L> dd = ldv<L>(a.invD, g);
-        FV<L> r, p;
-        if (MODE == 2 && act) {
+        const ColPPE32 P = ld_col(a.ppe32 + c);
+        const FV<L> dd = ldv<L>(a.invD, g), q0 = ldv<L>(a.r0, g);
+        const bool ldT = act && kk + L < NZI && (lane == 31 || h + 1 >= ngrp);
+        const bool ldB = act && kk > 0 && lane == 0;
+        const float eT = ldT ? pv_p1<MODE>(a, pin, vin, beta, om, g + L) : 0.f;
+        const float eB = ldB ? pv_p1<MODE>(a, pin, vin, beta, om, g - 1) : 0.f;
+        FV<L> r, p, e;
+        if (MODE == 2) {
             const FV<L> ss = ldv<L>(a.s, g), tt = ldv<L>(a.t, g), pp = ldv<L>(pin, g), vv = ldv<L>(vin, g);
-            FV<L> e = ldv<L>(a.e, g);
+            e = ldv<L>(a.e, g);
 #pragma unroll
             for (int l = 0; l < L; ++l) {
                 r[l] = fmaf(-om, tt[l], ss[l]);
                 p[l] = fmaf(beta, fmaf(-om, vv[l], pp[l]), r[l]);
                 // increment of the previous iteration: e += D^-1 (alpha p + omega s)
                 e[l] = e[l] + fmaf(om, ss[l], al * pp[l]);
-                f[1] += e[l];
-                const float ru = r[l] * __frcp_rn(dd[l]);  // unscaled r
-                f[3] += fabsf(ru);
-                f[4] = fmaf(ru, ru, f[4]);
             }
-            stv<L>(a.e, g, e);
-            stv<L>(a.r, g, r);
-        } else if (MODE == 2) {
-#pragma unroll
-            for (int l = 0; l < L; ++l) { r[l] = 0.f; p[l] = 0.f; }
         } else {
             r = ldv<L>(a.r, g);
             p = r;
@@ -212,24 +220,34 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
                 for (int l = 0; l < L; ++l) p[l] = fmaf(beta, fmaf(-om, vv[l], pp[l]), r[l]);
             }
         }
+        const FV<L> n1 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[0] - c) * NZI);
+        const FV<L> n2 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[1] - c) * NZI);
+        const FV<L> n3 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[2] - c) * NZI);
         float yT = __shfl_down_sync(0xffffffffu, p[0], 1);
         float yB = __shfl_up_sync(0xffffffffu, p[L - 1], 1);
         if (!act) continue;
         if (kk + L >= NZI) yT = 0.f;
-        else if (lane == 31 || h + 1 >= ngrp) yT = pv_p1<MODE>(a, pin, vin, beta, om, g + L);
+        else if (ldT) yT = eT;
         if (kk == 0) yB = 0.f;
-        else if (lane == 0) yB = pv_p1<MODE>(a, pin, vin, beta, om, g - 1);
-        const FV<L> n1 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[0] - c) * NZI);
-        const FV<L> n2 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[1] - c) * NZI);
-        const FV<L> n3 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[2] - c) * NZI);
+        else if (ldB) yB = eB;
         FV<L> v;
 #pragma unroll
         for (int l = 0; l < L; ++l)
-            v[l] = a_row32(a, nz, P, k0 + l, p[l], n1[l], n2[l], n3[l], (l + 1 < L) ? p[l + 1] : yT,
+            v[l] = a_row32(a, P, k0 + l, p[l], n1[l], n2[l], n3[l], (l + 1 < L) ? p[l + 1] : yT,
                            (l > 0) ? p[l - 1] : yB) * dd[l];  // v~ = D^-1 A p~
+        if (MODE == 2) {
+#pragma unroll
+            for (int l = 0; l < L; ++l) {
+                f[1] += e[l];
+                const float ru = r[l] * __frcp_rn(dd[l]);  // unscaled r
+                f[3] += fabsf(ru);
+                f[4] = fmaf(ru, ru, f[4]);
+            }
+            stv<L>(a.e, g, e);
+            stv<L>(a.r, g, r);
+        }
         stv<L>(pout, g, p);
         stv<L>(vout, g, v);
-        const FV<L> q0 = ldv<L>(a.r0, g);
 #pragma unroll
         for (int l = 0; l < L; ++l) {
             f[0] = fmaf(q0[l], v[l], f[0]);  // (r0, v) = (r^0, v~)
@@ -242,8 +260,11 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
 // In mode 2 it also forms the norms of r and takes the hand-over test: when
 // it fires, alpha is left as it was, so that the pass repeated after the FP64
 // update (mode 1, same iteration index) continues the same Krylov process.
+// Capped at 64 registers (4 blocks of 256 per SM instead of 3): the pass is
+// latency-bound and the extra resident warps outweigh a few spilled values
+// (8 % faster at 6.3M prisms).
 template <int L>
-__global__ void __launch_bounds__(kBlock) k_in_pv(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
+__global__ void __launch_bounds__(kBlock, 4) k_in_pv(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
     if (sc->done || sc->pending) return;
     const int it = sc->iiter;
     const int mode = (it == 0) ? 0 : (sc->rfresh ? 1 : 2);
@@ -286,7 +307,7 @@ __global__ void __launch_bounds__(kBlock) k_in_pv(Mesh m, MixArgs a, RedScratch 
 template <int L>
 __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
     if (sc->done || sc->pending) return;
-    const int it = sc->iiter, nz = m.NZ, NZI = m.NZI;
+    const int it = sc->iiter, NZI = m.NZI;
     const float al = (float)sc->ialpha;
     const float* v = (it & 1) ? a.v0 : a.v1;
     const int ngrp = m.nprism / L;
@@ -306,8 +327,16 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
         const int g = L * (act ? h : hw);
         const int c = g / NZI, kk = g - c * NZI;
         const int k0 = kk + 1;
-        const ColPPE32& P = a.ppe32[c];
-        const FV<L> rr = ldv<L>(a.r, g), vv = ldv<L>(v, g), dd = ldv<L>(a.invD, g);
+        // all loads of the group before the shuffle and the stores
+        const ColPPE32 P = ld_col(a.ppe32 + c);
+        const FV<L> rr = ldv<L>(a.r, g), vv = ldv<L>(v, g), dd = ldv<L>(a.invD, g), q0 = ldv<L>(a.r0, g);
+        const bool ldT = act && kk + L < NZI && (lane == 31 || h + 1 >= ngrp);
+        const bool ldB = act && kk > 0 && lane == 0;
+        const float eT = ldT ? z1(g + L) : 0.f;
+        const float eB = ldB ? z1(g - 1) : 0.f;
+        const FV<L> n1 = zv(g + (size_t)(P.nb[0] - c) * NZI);
+        const FV<L> n2 = zv(g + (size_t)(P.nb[1] - c) * NZI);
+        const FV<L> n3 = zv(g + (size_t)(P.nb[2] - c) * NZI);
         FV<L> z0;
 #pragma unroll
         for (int l = 0; l < L; ++l) z0[l] = fmaf(-al, vv[l], rr[l]);
@@ -315,23 +344,19 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
         float zB = __shfl_up_sync(0xffffffffu, z0[L - 1], 1);
         if (!act) continue;
         if (kk + L >= NZI) zT = 0.f;
-        else if (lane == 31 || h + 1 >= ngrp) zT = z1(g + L);
+        else if (ldT) zT = eT;
         if (kk == 0) zB = 0.f;
-        else if (lane == 0) zB = z1(g - 1);
-        const FV<L> n1 = zv(g + (size_t)(P.nb[0] - c) * NZI);
-        const FV<L> n2 = zv(g + (size_t)(P.nb[1] - c) * NZI);
-        const FV<L> n3 = zv(g + (size_t)(P.nb[2] - c) * NZI);
+        else if (ldB) zB = eB;
         FV<L> t;
 #pragma unroll
         for (int l = 0; l < L; ++l)
-            t[l] = a_row32(a, nz, P, k0 + l, z0[l], n1[l], n2[l], n3[l], (l + 1 < L) ? z0[l + 1] : zT,
+            t[l] = a_row32(a, P, k0 + l, z0[l], n1[l], n2[l], n3[l], (l + 1 < L) ? z0[l + 1] : zT,
                            (l > 0) ? z0[l - 1] : zB);
         FV<L> tt;
 #pragma unroll
         for (int l = 0; l < L; ++l) tt[l] = t[l] * dd[l];
         stv<L>(a.s, g, z0);
         stv<L>(a.t, g, tt);
-        const FV<L> q0 = ldv<L>(a.r0, g);
 #pragma unroll
         for (int l = 0; l < L; ++l) {
             const float su = z0[l] * __frcp_rn(dd[l]);  // unscaled s
@@ -586,7 +611,7 @@ int mixed_alloc(nsmp_ctx* c) {
     CK(dalloc((void**)&c->invD32, 2 * ncf * sizeof(float)));
     c->r032 = c->invD32 + ncf;
     CK(dalloc((void**)&c->d_ppe32, sizeof(ColPPE32) * L.N0));
-    CK(dalloc((void**)&c->lev32, sizeof(float) * 3 * L.NZ));
+    CK(dalloc((void**)&c->lev32, sizeof(float) * 4 * L.NZ));
     std::vector<ColPPE32> p32(L.N0);
     for (int q = 0; q < L.N0; ++q) {
         for (int j = 0; j < 3; ++j) {
@@ -596,11 +621,11 @@ int mixed_alloc(nsmp_ctx* c) {
         p32[q].area = (float)L.ppe[q].area;
         p32[q].pad = 0.f;
     }
-    std::vector<float> lv(3 * (size_t)L.NZ, 0.f);
+    std::vector<float> lv(4 * (size_t)L.NZ, 0.f);  // one float4 per level
     for (int k = 1; k <= L.NZ - 2; ++k) {
-        lv[k] = (float)L.lev.dsv[k];
-        lv[L.NZ + k] = (float)(L.lev.idsT[k] * L.lev.wT[k]);
-        lv[2 * L.NZ + k] = (float)(L.lev.idsB[k] * L.lev.wB[k]);
+        lv[4 * k] = (float)L.lev.dsv[k];
+        lv[4 * k + 1] = (float)(L.lev.idsT[k] * L.lev.wT[k]);
+        lv[4 * k + 2] = (float)(L.lev.idsB[k] * L.lev.wB[k]);
     }
     CK(cudaMemcpyAsync(c->d_ppe32, p32.data(), sizeof(ColPPE32) * L.N0, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->lev32, lv.data(), sizeof(float) * lv.size(), cudaMemcpyHostToDevice, c->stream));
@@ -669,7 +694,8 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     const int g_in = grid_occ(c, k_mix_init, m.nprism), g_u = grid_occ(c, k_mix_update, m.nprism);
     const int g_sc = grid_occ(c, k_mix_scale, m.nprism), g_sh = grid_occ(c, k_mix_shadow, m.nprism);
     MixArgs a{c->rhsp, pf, c->b64, c->r, c->x, c->xa, c->xb, c->r32, c->r032, c->p32[0], c->p32[1], c->v32[0],
-              c->v32[1], c->s32, c->t32, c->e32, c->invD32, c->d_ppe32, c->lev32};
+              c->v32[1], c->s32, c->t32, c->e32, c->invD32, c->d_ppe32,
+              reinterpret_cast<const float4*>(c->lev32)};
     CK(cudaMemcpyAsync(&c->d_scal->inner_tol, &c->inner_tol, sizeof(double), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(&c->d_scal->inner_cap, &c->inner_cap, sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(&c->d_scal->restart_every, &c->restart_every, sizeof(int), cudaMemcpyHostToDevice, st));
