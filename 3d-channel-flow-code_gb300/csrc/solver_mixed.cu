@@ -49,7 +49,15 @@ struct MixArgs {
     float *r, *r0, *p0, *p1, *v0, *v1, *s, *t, *e;
     const float* invD;
     const ColPPE32* ppe32;
-    const float4* lev32; // per level k0: {dsigv(k-1), wT/dsig(k), wB/dsig(k-1), 0}
+    // The level factors dsigv(k-1), wT/dsig(k), wB/dsig(k-1) of the operator
+    // in two layouts.  lev32: three rows of nzp floats indexed by the interior
+    // layer kk = k0 - 1, so a thread's L layers are one aligned vector per row
+    // (3 loads a group; the s/t pass).  lev4: one float4 per level k0, loaded
+    // where each layer's row is formed (fewer live registers; the p/v pass,
+    // which runs at its register cap).
+    const float* lev32;
+    int nzp;
+    const float4* lev4;
 };
 
 // The 32-byte column record as two 16-byte loads.
@@ -63,12 +71,12 @@ __device__ __forceinline__ ColPPE32 ld_col(const ColPPE32* p) {
     return P;
 }
 
-// FP32 operator row: A y at one prism (same coefficients as ppe_row).
-__device__ __forceinline__ float a_row32(const MixArgs& a, const ColPPE32& P, int k0, float y0, float y1, float y2,
+// FP32 operator row: A y at one prism (same coefficients as ppe_row), from
+// the level factors dsv, aT, aB of its layer.
+__device__ __forceinline__ float a_row32(const ColPPE32& P, float dsv, float aT, float aB, float y0, float y1, float y2,
                                          float y3, float yT, float yB) {
-    const float4 q = __ldg(a.lev32 + k0);
-    const float AA1 = P.kA[0] * q.x, AA2 = P.kA[1] * q.x, AA3 = P.kA[2] * q.x;
-    const float AAT = P.area * q.y, AAB = P.area * q.z;
+    const float AA1 = P.kA[0] * dsv, AA2 = P.kA[1] * dsv, AA3 = P.kA[2] * dsv;
+    const float AAT = P.area * aT, AAB = P.area * aB;
     const float AA0 = -(AAT + AAB + AA1 + AA2 + AA3);
     return AA0 * y0 + AA1 * y1 + AA2 * y2 + AA3 * y3 + AAT * yT + AAB * yB;
 }
@@ -193,7 +201,6 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
         const bool act = h < ngrp;
         const int g = L * (act ? h : hw);
         const int c = g / NZI, kk = g - c * NZI;  // layers k0 = kk+1 .. kk+L
-        const int k0 = kk + 1;
         const ColPPE32 P = ld_col(a.ppe32 + c);
         const FV<L> dd = ldv<L>(a.invD, g), q0 = ldv<L>(a.r0, g);
         const bool ldT = act && kk + L < NZI && (lane == 31 || h + 1 >= ngrp);
@@ -232,9 +239,11 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
         else if (ldB) yB = eB;
         FV<L> v;
 #pragma unroll
-        for (int l = 0; l < L; ++l)
-            v[l] = a_row32(a, P, k0 + l, p[l], n1[l], n2[l], n3[l], (l + 1 < L) ? p[l + 1] : yT,
+        for (int l = 0; l < L; ++l) {
+            const float4 q = __ldg(a.lev4 + kk + 1 + l);
+            v[l] = a_row32(P, q.x, q.y, q.z, p[l], n1[l], n2[l], n3[l], (l + 1 < L) ? p[l + 1] : yT,
                            (l > 0) ? p[l - 1] : yB) * dd[l];  // v~ = D^-1 A p~
+        }
         if (MODE == 2) {
 #pragma unroll
             for (int l = 0; l < L; ++l) {
@@ -326,10 +335,10 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
         const bool act = h < ngrp;
         const int g = L * (act ? h : hw);
         const int c = g / NZI, kk = g - c * NZI;
-        const int k0 = kk + 1;
         // all loads of the group before the shuffle and the stores
         const ColPPE32 P = ld_col(a.ppe32 + c);
         const FV<L> rr = ldv<L>(a.r, g), vv = ldv<L>(v, g), dd = ldv<L>(a.invD, g), q0 = ldv<L>(a.r0, g);
+        const FV<L> ls = ldv<L>(a.lev32, kk), lt = ldv<L>(a.lev32, a.nzp + kk), lb = ldv<L>(a.lev32, 2 * a.nzp + kk);
         const bool ldT = act && kk + L < NZI && (lane == 31 || h + 1 >= ngrp);
         const bool ldB = act && kk > 0 && lane == 0;
         const float eT = ldT ? z1(g + L) : 0.f;
@@ -350,7 +359,7 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
         FV<L> t;
 #pragma unroll
         for (int l = 0; l < L; ++l)
-            t[l] = a_row32(a, P, k0 + l, z0[l], n1[l], n2[l], n3[l], (l + 1 < L) ? z0[l + 1] : zT,
+            t[l] = a_row32(P, ls[l], lt[l], lb[l], z0[l], n1[l], n2[l], n3[l], (l + 1 < L) ? z0[l + 1] : zT,
                            (l > 0) ? z0[l - 1] : zB);
         FV<L> tt;
 #pragma unroll
@@ -611,7 +620,8 @@ int mixed_alloc(nsmp_ctx* c) {
     CK(dalloc((void**)&c->invD32, 2 * ncf * sizeof(float)));
     c->r032 = c->invD32 + ncf;
     CK(dalloc((void**)&c->d_ppe32, sizeof(ColPPE32) * L.N0));
-    CK(dalloc((void**)&c->lev32, sizeof(float) * 4 * L.NZ));
+    const int nzp = (L.NZ - 2 + 3) / 4 * 4;  // interior layers, rounded up to a float4
+    CK(dalloc((void**)&c->lev32, sizeof(float) * (3 * nzp + 4 * (size_t)L.NZ)));
     std::vector<ColPPE32> p32(L.N0);
     for (int q = 0; q < L.N0; ++q) {
         for (int j = 0; j < 3; ++j) {
@@ -621,11 +631,16 @@ int mixed_alloc(nsmp_ctx* c) {
         p32[q].area = (float)L.ppe[q].area;
         p32[q].pad = 0.f;
     }
-    std::vector<float> lv(4 * (size_t)L.NZ, 0.f);  // one float4 per level
+    // rows indexed by the interior layer k0 - 1, then one float4 per level k0
+    std::vector<float> lv(3 * (size_t)nzp + 4 * (size_t)L.NZ, 0.f);
+    float* l4 = lv.data() + 3 * nzp;
     for (int k = 1; k <= L.NZ - 2; ++k) {
-        lv[4 * k] = (float)L.lev.dsv[k];
-        lv[4 * k + 1] = (float)(L.lev.idsT[k] * L.lev.wT[k]);
-        lv[4 * k + 2] = (float)(L.lev.idsB[k] * L.lev.wB[k]);
+        const float f[3] = {(float)L.lev.dsv[k], (float)(L.lev.idsT[k] * L.lev.wT[k]),
+                            (float)(L.lev.idsB[k] * L.lev.wB[k])};
+        for (int j = 0; j < 3; ++j) {
+            lv[j * nzp + k - 1] = f[j];
+            l4[4 * k + j] = f[j];
+        }
     }
     CK(cudaMemcpyAsync(c->d_ppe32, p32.data(), sizeof(ColPPE32) * L.N0, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->lev32, lv.data(), sizeof(float) * lv.size(), cudaMemcpyHostToDevice, c->stream));
@@ -694,8 +709,8 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     const int g_in = grid_occ(c, k_mix_init, m.nprism), g_u = grid_occ(c, k_mix_update, m.nprism);
     const int g_sc = grid_occ(c, k_mix_scale, m.nprism), g_sh = grid_occ(c, k_mix_shadow, m.nprism);
     MixArgs a{c->rhsp, pf, c->b64, c->r, c->x, c->xa, c->xb, c->r32, c->r032, c->p32[0], c->p32[1], c->v32[0],
-              c->v32[1], c->s32, c->t32, c->e32, c->invD32, c->d_ppe32,
-              reinterpret_cast<const float4*>(c->lev32)};
+              c->v32[1], c->s32, c->t32, c->e32, c->invD32, c->d_ppe32, c->lev32,
+              (m.NZI + 3) / 4 * 4, reinterpret_cast<const float4*>(c->lev32 + 3 * ((m.NZI + 3) / 4 * 4))};
     CK(cudaMemcpyAsync(&c->d_scal->inner_tol, &c->inner_tol, sizeof(double), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(&c->d_scal->inner_cap, &c->inner_cap, sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(&c->d_scal->restart_every, &c->restart_every, sizeof(int), cudaMemcpyHostToDevice, st));
