@@ -651,9 +651,12 @@ int mixed_alloc(nsmp_ctx* c) {
 }
 
 // L2 residency of D^-1 and r0 (the contiguous block of mixed_alloc) for the
-// kernels of one mixed solve: persisting up to the set-aside the device
-// allows, streaming beyond it.  off() returns the stream and the persisting
-// lines to normal use.
+// kernels of one mixed solve, only when the whole block fits the persisting
+// set-aside the device allows.  A partial window (hit ratio below 1) on a
+// block larger than that carves persisting lines out of the L2 that the
+// neighbour gathers of both passes rely on: at 33.5M prisms (a 268 MB block)
+// it made the FP32 iteration 1.8x slower.  The destructor returns the stream
+// and the persisting lines to normal use.
 struct L2Window {
     nsmp_ctx* c;
     bool on = false;
@@ -663,7 +666,8 @@ struct L2Window {
         cudaDeviceGetAttribute(&maxwin, cudaDevAttrMaxAccessPolicyWindowSize, dev);
         cudaDeviceGetAttribute(&maxpers, cudaDevAttrMaxPersistingL2CacheSize, dev);
         if (maxwin <= 0 || maxpers <= 0) return;
-        const size_t win = std::min(bytes, (size_t)maxwin);
+        if (bytes > (size_t)maxwin || bytes > (size_t)maxpers) return;
+        const size_t win = bytes;
         size_t lim = 0;
         if (cudaDeviceGetLimit(&lim, cudaLimitPersistingL2CacheSize) != cudaSuccess) return;
         if (lim < std::min(win, (size_t)maxpers)) {
