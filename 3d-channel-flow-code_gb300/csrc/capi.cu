@@ -93,29 +93,28 @@ int nsmp_upload_state(nsmp_ctx* c, const double* u, const double* v, const doubl
                       const double* ubf, const double* rhsu, const double* rhsv, const double* rhsw, int flag_ab) {
     if (!c || !u || !v || !w || !p || !u1f || !u2f || !u3f || !utf || !ubf || !rhsu || !rhsv || !rhsw)
         return NSMP_ERR_ARG;
+    // one contiguous copy and a scatter per array, one synchronisation at the
+    // end (the host arrays are free for reuse when this returns)
     const double* cells[4] = {u, v, w, p};
     for (int f = 0; f < 4; ++f) {
-        int rc = nsmp::run_scatter(c, cells[f], c->lvl[c->ln][f]);
+        int rc = nsmp::run_scatter(c, cells[f], c->lvl[c->ln][f], c->L.NC, false);
         if (rc) return rc;
     }
     int rc = nsmp::run_fill_ghosts(c, c->ln);
     if (rc) return rc;
-    // face fluxes are (N0,NZ): same layout as the interior rows of a cell field
+    // face fluxes are (N0,NZ)
     const double* faces[5] = {u1f, u2f, u3f, utf, ubf};
-    const int ncell = c->L.NC;
     for (int f = 0; f < 5; ++f) {
-        // widen (N0,NZ) to (N_CELL,NZ) rows on the host side of the staging copy
-        std::vector<double> tmp((size_t)ncell * c->L.NZ, 0.0);
-        for (int k = 0; k < c->L.NZ; ++k)
-            std::memcpy(&tmp[(size_t)k * ncell], faces[f] + (size_t)k * c->L.N0, sizeof(double) * c->L.N0);
-        rc = nsmp::run_scatter(c, tmp.data(), c->face[f]);
+        rc = nsmp::run_scatter(c, faces[f], c->face[f], c->L.N0, false);
         if (rc) return rc;
     }
     const double* hs[3] = {rhsu, rhsv, rhsw};
     for (int f = 0; f < 3; ++f) {
-        rc = nsmp::run_scatter(c, hs[f], c->hist[f]);
+        rc = nsmp::run_scatter(c, hs[f], c->hist[f], c->L.NC, false);
         if (rc) return rc;
     }
+    const cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return set_err(c, NSMP_ERR_CUDA, std::string("upload_state: ") + cudaGetErrorString(e));
     c->flag_ab = flag_ab;
     c->lknown = c->ln;
     return NSMP_OK;

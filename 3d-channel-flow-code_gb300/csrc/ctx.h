@@ -88,7 +88,7 @@ int run_user_initial(nsmp_ctx* c);
 int run_fill_ghosts(nsmp_ctx* c, int buf);
 int run_combine(nsmp_ctx* c, double a, double b);
 int run_gather(nsmp_ctx* c, const double* dfield, int ghost_mode, int rows, double* host);
-int run_scatter(nsmp_ctx* c, const double* host, double* dfield);
+int run_scatter(nsmp_ctx* c, const double* host, double* dfield, int rows = 0, bool sync = true);
 int run_mass_diag(nsmp_ctx* c, double out[4]);
 int run_mass_diag_noalloc(nsmp_ctx* c, double out[4]);
 int run_download_pv(nsmp_ctx* c, double* host);

@@ -348,12 +348,13 @@ __global__ void k_gather(int ncell, int nz, int layers, int kofs, const int* __r
     }
 }
 
-__global__ void k_scatter(int n0, int nz, const int* __restrict__ col, const double* __restrict__ in,
+// in is a (rows,NZ) Fortran array; its first n0 rows go to the columns.
+__global__ void k_scatter(int n0, int nz, int rows, const int* __restrict__ col, const double* __restrict__ in,
                           double* __restrict__ f) {
     const size_t n = (size_t)n0 * nz;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const int cell = (int)(i % n0), k = (int)(i / n0);
-        f[(size_t)col[cell] * nz + k] = in[(size_t)cell + (size_t)k * n0];
+        f[(size_t)col[cell] * nz + k] = in[(size_t)cell + (size_t)k * rows];
     }
 }
 
@@ -600,17 +601,23 @@ int run_download_pv(nsmp_ctx* c, double* host) {
     return 0;
 }
 
-// host (N_CELL,NZ) interior rows -> device columns
-int run_scatter(nsmp_ctx* c, const double* host, double* dfield) {
-    const int ncell = c->L.NC, n0 = c->L.N0, nz = c->mesh.NZ;
-    // copy the interior rows column by column of the Fortran array
-    for (int k = 0; k < nz; ++k)
-        CK(cudaMemcpyAsync(c->stage_buf + (size_t)k * n0, host + (size_t)k * ncell, n0 * sizeof(double),
-                           cudaMemcpyHostToDevice, c->stream));
-    // stage_buf now holds an (N0,NZ) array; scatter into columns
-    k_scatter<<<grid_for(c, (long long)n0 * nz), kBlock, 0, c->stream>>>(n0, nz, c->d_gather, c->stage_buf, dfield);
+// Host (rows,NZ) Fortran array -> device columns, rows = N_CELL (cell
+// fields, ghost rows ignored) or N0 (face fluxes): one contiguous copy into
+// the staging buffer and a scatter of the interior rows.  Without sync the
+// caller synchronises the stream before the host array may change; copies
+// of consecutive calls are ordered behind the previous scatter on the stream.
+int run_scatter(nsmp_ctx* c, const double* host, double* dfield, int rows, bool sync) {
+    const int n0 = c->L.N0, nz = c->mesh.NZ;
+    if (rows <= 0) rows = c->L.NC;
+    if (rows < n0 || rows > c->L.NC) {
+        c->err = "run_scatter: rows out of range";
+        return NSMP_ERR_ARG;
+    }
+    CK(cudaMemcpyAsync(c->stage_buf, host, (size_t)rows * nz * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    k_scatter<<<grid_for(c, (long long)n0 * nz), kBlock, 0, c->stream>>>(n0, nz, rows, c->d_gather, c->stage_buf,
+                                                                         dfield);
     CKL("k_scatter");
-    CK(cudaStreamSynchronize(c->stream));
+    if (sync) CK(cudaStreamSynchronize(c->stream));
     return 0;
 }
 

@@ -271,8 +271,14 @@ class Solver:
         self._check(self.L.nsmp_upload_state(self.h, *[_p(a) for a in arrs], int(flag_ab)))
         self.flag_ab = int(flag_ab)
 
-    def download(self, field):
-        out = np.zeros(self.shape(field), dtype=np.float64, order="F")
+    def download(self, field, out=None):
+        """Field in the reference's Fortran layout; into `out` (float64,
+        Fortran-ordered, of the field's shape, e.g. pinned memory) if given."""
+        shape = tuple(self.shape(field))
+        if out is None:
+            out = np.zeros(shape, dtype=np.float64, order="F")
+        elif out.dtype != np.float64 or out.shape != shape or not out.flags.f_contiguous:
+            raise ValueError("out must be a Fortran-ordered float64 array of shape %s" % (shape,))
         self._check(self.L.nsmp_download(self.h, field, _p(out)))
         return out
 

@@ -218,6 +218,35 @@ WORDS_MIXED = {
 }
 
 
+class StateBuffers:
+    """The full restart state of a solver (u, v, w, p, five face fluxes, three
+    AB2 histories, the AB2 flag) in pinned host arrays in the reference's
+    Fortran layout."""
+
+    CELLS = ("F_U", "F_V", "F_W", "F_P")
+    FACES = ("F_U1FACE", "F_U2FACE", "F_U3FACE", "F_UTFACE", "F_UBFACE")
+    HIST = ("F_RHSU", "F_RHSV", "F_RHSW")
+
+    def __init__(self, torch, ng, s, prm):
+        pin = lambda shape: torch.empty(shape[::-1], dtype=torch.float64, pin_memory=True).numpy().T
+        nc, nz, n0 = s.ncell, s.nz, prm["n0"]
+        self.ids = [[getattr(ng, n) for n in grp] for grp in (self.CELLS, self.FACES, self.HIST)]
+        self.cells = [pin((nc, nz)) for _ in self.CELLS]
+        self.faces = [pin((n0, nz)) for _ in self.FACES]
+        self.hist = [pin((nc, nz)) for _ in self.HIST]
+        self.flag = 0
+        self.nbytes = sum(a.nbytes for a in self.cells + self.faces + self.hist)
+
+    def download(self, s):
+        for grp, ids in zip((self.cells, self.faces, self.hist), self.ids):
+            for a, f in zip(grp, ids):
+                s.download(f, out=a)
+        self.flag = s.flag_ab
+
+    def upload(self, s, flag):
+        s.upload_state(*self.cells, self.faces, self.hist, flag)
+
+
 def timed_region(s, ng, torch, stream, steps, pg, local, profile=False):
     """K RK3 steps between CUDA events on the library's stream.  With
     profile=True the library also records an event pair around each of its
@@ -291,7 +320,9 @@ def run_ours(args):
     prisms = 2 * nx * ny * layers
     mesh = ng.make_mesh(nx, ny)
     precs = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
+    head = "mixed" if "mixed" in precs else precs[0]
     res, solvers = {}, {}
+    snap = u_end = None
     for prec in precs:
         prm = ng.channel_params(nx, ny, layers, dt, device=local,
                                 precision=(ng.MIXED if prec == "mixed" else ng.FP64))
@@ -303,7 +334,12 @@ def run_ours(args):
             rc, _ = s.step(3, 1)
             if rc < 0:
                 raise RuntimeError(f"warm-up step failed: {rc}")
+        if prec == head:  # the state the timed steps start from, for the end-to-end replay
+            snap = StateBuffers(torch, ng, s, prm)
+            snap.download(s)
         r = timed_region(s, ng, torch, stream, args.steps, pg, local)
+        if prec == head:
+            u_end = s.download(ng.F_U)
         r["ms_max"] = max_over_ranks(pg, r["ms"])
         r["value"] = job_value(world, prisms, args.steps, r["ms_max"])
         # per-kernel device times over K further steps of the same run
@@ -312,7 +348,6 @@ def run_ours(args):
         r["roof"], r["shares"], r["busy_ms"] = roofline(rp["prof"], rp["iters"], prisms, prec == "mixed")
         res[prec] = r
         solvers[prec] = (s, stream, prm)
-    head = "mixed" if "mixed" in res else precs[0]
     s, stream, prm = solvers[head]
     r = res[head]
 
@@ -338,34 +373,29 @@ def run_ours(args):
         cmp["speedup"] = res["mixed"]["value"] / res["fp64"]["value"]
         cmp["after_steps"] = args.warmup + 2 * args.steps
 
-    # ---- end to end through the C-ABI with host buffers -------------------
-    pin = lambda shape: torch.empty(shape[::-1], dtype=torch.float64, pin_memory=True).numpy().T
-    nc, nz = s.ncell, s.nz
-    h_cells = [pin((nc, nz)) for _ in range(4)]
-    h_faces = [pin((prm["n0"], nz)) for _ in range(5)]
-    h_hist = [pin((nc, nz)) for _ in range(3)]
-    for hh, f in zip(h_cells, (ng.F_U, ng.F_V, ng.F_W, ng.F_P)):
-        hh[...] = s.download(f)
-    for hh, f in zip(h_faces, (ng.F_U1FACE, ng.F_U2FACE, ng.F_U3FACE, ng.F_UTFACE, ng.F_UBFACE)):
-        hh[...] = s.download(f)
-    for hh, f in zip(h_hist, (ng.F_RHSU, ng.F_RHSV, ng.F_RHSW)):
-        hh[...] = s.download(f)
-    h_out = [pin((nc, nz)) for _ in range(4)]
-    flag = s.flag_ab
-    e2e_steps = max(1, min(args.steps, 3))
+    # ---- end to end: the timed steps replayed through the C-ABI -------------
+    # From the state the timed region started from, every step uploads its
+    # full input state from pinned host memory, steps, and downloads its full
+    # output state, which is the next step's input.  The K steps are those of
+    # the timed region, so the solver work is the same and the copies are
+    # what is added; the replay ends on the timed region's final u, bit for
+    # bit, when upload and download are exact.
+    st_out = StateBuffers(torch, ng, s, prm)
+    st_in, flag = snap, snap.flag
     torch.cuda.synchronize()
     barrier(pg)
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        s.upload_state(*h_cells, h_faces, h_hist, flag)
+    for _ in range(args.steps):
+        st_in.upload(s, flag)
         s.step(3, 1)
-        for hh, f in zip(h_out, (ng.F_U, ng.F_V, ng.F_W, ng.F_P)):
-            hh[...] = s.download(f)
+        st_out.download(s)
+        flag = st_out.flag
+        st_in, st_out = st_out, st_in
     torch.cuda.synchronize()
     t_e2e = max_over_ranks(pg, time.perf_counter() - t0)
-    e2e_value = job_value(world, prisms, e2e_steps, t_e2e * 1e3)
-    h2d = (4 * nc * nz + 5 * prm["n0"] * nz + 3 * nc * nz) * 8
-    d2h = 4 * nc * nz * 8
+    e2e_value = job_value(world, prisms, args.steps, t_e2e * 1e3)
+    e2e_exact = bool(np.array_equal(st_in.cells[0], u_end))
+    h2d = d2h = st_in.nbytes
 
     # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
     cpu = None
@@ -394,7 +424,9 @@ def run_ours(args):
             "device_busy_frac": round(r["busy_ms"] / max(r["prof_ms"], 1e-9), 4),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+                    "d2h_bytes_per_step": d2h, "steps": args.steps,
+                    "replay": "the timed steps from their start state, full state up and down each step",
+                    "replay_matches_timed_u_bitwise": e2e_exact},
             "clocks": r["clocks"],
             "gpu_launches": r["launches"],
             "status": r["status"],

@@ -184,6 +184,32 @@ def test_upload_state_restart():
         assert rel_l2(s2.download(f), s1.download(f)) <= 1e-12
 
 
+def test_upload_download_roundtrip_is_exact():
+    """Every array of nsmp_upload_state comes back bit for bit (interior rows
+    and layers; ghosts are rebuilt), also into a caller's buffer."""
+    prm, mesh = small_case(8, 6, layers=6)
+    s = ng.Solver(prm, mesh)
+    rng = np.random.default_rng(11)
+    n0, nc, nz = prm["n0"], s.ncell, s.nz
+    cells = [np.asfortranarray(rng.standard_normal((nc, nz))) for _ in range(4)]
+    faces = [np.asfortranarray(rng.standard_normal((n0, nz))) for _ in range(5)]
+    hist = [np.asfortranarray(rng.standard_normal((nc, nz))) for _ in range(3)]
+    s.upload_state(*cells, faces, hist, 1)
+    cell_ids = (ng.F_U, ng.F_V, ng.F_W, ng.F_P, ng.F_RHSU, ng.F_RHSV, ng.F_RHSW)
+    for a, f in zip(cells + hist, cell_ids):
+        b = s.download(f)
+        assert np.array_equal(b[:n0, 1:-1], a[:n0, 1:-1]), f
+        out = np.full((nc, nz), np.nan, order="F")
+        assert s.download(f, out=out) is out
+        assert np.array_equal(out, b)
+    face_ids = (ng.F_U1FACE, ng.F_U2FACE, ng.F_U3FACE, ng.F_UTFACE, ng.F_UBFACE)
+    for a, f in zip(faces, face_ids):
+        assert np.array_equal(s.download(f)[:, 1:-1], a[:, 1:-1]), f
+    with pytest.raises(ValueError):
+        s.download(ng.F_U, out=np.zeros((nc, nz)))  # C order
+    s.close()
+
+
 @pytest.mark.slow
 def test_config0_100_steps():
     """configs[0]: 100 RK3 steps, relative L2 <= 1e-8 per field."""
