@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
         stv<L>(a.t, g, tt);
 #pragma unroll
         for (int l = 0; l < L; ++l) {
-            const float su = z0[l] * __frcp_rn(dd[l]);  // unscaled s
+            const float su = __fdividef(z0[l], dd[l]);  // unscaled s (2 ulp: it only enters omega)
             f[0] = fmaf(t[l], su, f[0]);       // (t, s)
             f[1] = fmaf(t[l], t[l], f[1]);     // (t, t)
             f[2] = fmaf(q0[l], z0[l], f[2]);   // (r0, s) = (r^0, s~)
