@@ -43,6 +43,9 @@ struct nsmp_ctx {
     double *b64 = nullptr, *xa = nullptr, *xb = nullptr;
     float *r32 = nullptr, *r032 = nullptr, *p32[2] = {}, *v32[2] = {}, *s32 = nullptr, *t32 = nullptr,
           *e32 = nullptr, *invD32 = nullptr, *lev32 = nullptr;
+    // double-float (hi, lo) copies of the PPE coefficients for the FP64
+    // hand-over: per column {kA1..3, area}, per level {dsigv, aT, aB, 0}
+    float *ddcol = nullptr, *ddlev = nullptr;
     nsmp::ColPPE32* d_ppe32 = nullptr;
     int l2_limit_set = 0;         // 1: this context raised the persisting-L2 limit (reset at destroy)
     double inner_tol = 1e-1;      // FP32 residual reduction that triggers an FP64 update

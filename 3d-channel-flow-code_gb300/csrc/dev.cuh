@@ -168,6 +168,43 @@ __device__ bool grid_reduce(double (&x)[N], RedScratch rs, double (&tot)[N]) {
     return grid_finish<N, MAX>(x, rs, tot);
 }
 
+// Double-float arithmetic: a value is an unevaluated sum h + l of two FP32
+// numbers with |l| <= ulp(h)/2, about 48 significant bits.  The algorithms
+// are the published error-free transformations: TwoSum (Knuth, TAOCP vol. 2),
+// Fast2Sum (Dekker 1971), the FMA-based exact product, and the accurate
+// double-double addition of Hida, Li and Bailey (2001).  Every operation is
+// an explicitly rounded intrinsic, so the compiler cannot contract or
+// reorder the error terms away.  Used where FP64 issue rate, not accuracy,
+// is the constraint (about 2 FP64 instructions per SM clock on this GPU).
+struct F2 {
+    float h, l;
+};
+__device__ __forceinline__ F2 two_sum(float a, float b) {  // exact: a + b = s + e
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+__device__ __forceinline__ F2 fast_two_sum(float a, float b) {  // exact when |a| >= |b| or a == 0
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ F2 df_add(F2 a, F2 b) {
+    F2 s = two_sum(a.h, b.h);
+    const F2 t = two_sum(a.l, b.l);
+    s.l = __fadd_rn(s.l, t.h);
+    s = fast_two_sum(s.h, s.l);
+    s.l = __fadd_rn(s.l, t.l);
+    return fast_two_sum(s.h, s.l);
+}
+__device__ __forceinline__ F2 df_mul(F2 a, F2 b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);  // exact error of the product
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return fast_two_sum(p, e);
+}
+
 // Grid sum of FP32 per-thread values: FP32 inside each warp (a 32-value tree,
 // relative error at most 5 units of FP32 rounding), FP64 across warps and
 // blocks.  Used by the FP32 inner solver, whose values are formed in FP32

@@ -58,6 +58,11 @@ struct MixArgs {
     const float* lev32;
     int nzp;
     const float4* lev4;
+    // double-float PPE coefficients, two float4 each: per column
+    // {kA1 h,l, kA2 h,l}, {kA3 h,l, area h,l}; per level k0
+    // {dsigv h,l, aT h,l}, {aB h,l, 0, 0}
+    const float4* ddcol;
+    const float4* ddlev;
 };
 
 // The 32-byte column record as two 16-byte loads.
@@ -443,23 +448,33 @@ __global__ void __launch_bounds__(kBlock) k_mix_update(Mesh m, MixArgs a, RedScr
             x0 = xin[q];
             r = rin[q];
         } else {
-            // x1 = x + iscale c with c = e - mean e exactly as stored, and
-            // r1 = r - iscale A c in FP64 from the differences of c (A 1 = 0):
-            // the residual of the stored x1, at ~25 FP64 instructions a prism
-            auto cv = [&](size_t i) {
+            // x1 = x + iscale c with c = e - mean e exactly as stored (FP32),
+            // and r1 = r - iscale A c from the differences of c (A 1 = 0): the
+            // residual of the stored x1.  A c is formed in double-float FP32
+            // arithmetic (about 2^-44 relative): the differences are exact
+            // (TwoSum) and the coefficients are hi/lo splits of the FP64
+            // ones, so FP64 is left with the x and r updates and the norms
+            // (about 9 FP64 instructions a prism instead of 28).
+            auto cf = [&](size_t i) {
                 float e = a.e[i];
                 if (einc) e = e + fmaf(om, a.s[i], al * pl[i]);  // D^-1 (alpha p + omega s)
-                return (double)(e - em);
+                return e - em;
             };
-            const double c0 = cv(q);
-            const double dT = (k0 < m.NZ - 2) ? cv(q + 1) - c0 : 0.0;
-            const double dB = (k0 > 1) ? cv(q - 1) - c0 : 0.0;
-            const double d1 = cv(ICg(m, P.nb[0], k0)) - c0, d2 = cv(ICg(m, P.nb[1], k0)) - c0,
-                         d3 = cv(ICg(m, P.nb[2], k0)) - c0;
-            const double Ac = lev(m, LV_DSV, k0) * (P.kA[0] * d1 + P.kA[1] * d2 + P.kA[2] * d3) +
-                              P.area * (lev(m, LV_ATOP, k0) * dT + lev(m, LV_ABOT, k0) * dB);
-            x0 = fma(scale, c0, xin[q]);
-            r = fma(-scale, Ac, rin[q]);
+            const float c0 = cf(q);
+            const F2 zero = {0.f, 0.f};
+            const F2 dT = (k0 < m.NZ - 2) ? two_sum(cf(q + 1), -c0) : zero;
+            const F2 dB = (k0 > 1) ? two_sum(cf(q - 1), -c0) : zero;
+            const F2 d1 = two_sum(cf(ICg(m, P.nb[0], k0)), -c0), d2 = two_sum(cf(ICg(m, P.nb[1], k0)), -c0),
+                     d3 = two_sum(cf(ICg(m, P.nb[2], k0)), -c0);
+            const float4 ca = __ldg(a.ddcol + 2 * c), cb = __ldg(a.ddcol + 2 * c + 1);
+            const float4 la = __ldg(a.ddlev + 2 * k0), lb = __ldg(a.ddlev + 2 * k0 + 1);
+            F2 hz = df_add(df_add(df_mul({ca.x, ca.y}, d1), df_mul({ca.z, ca.w}, d2)), df_mul({cb.x, cb.y}, d3));
+            hz = df_mul({la.x, la.y}, hz);
+            F2 vt = df_add(df_mul({la.z, la.w}, dT), df_mul({lb.x, lb.y}, dB));
+            vt = df_mul({cb.z, cb.w}, vt);
+            const F2 Ac = df_add(hz, vt);
+            x0 = fma(scale, (double)c0, xin[q]);
+            r = fma(-scale, (double)Ac.h + (double)Ac.l, rin[q]);
         }
         xout[q] = x0;
         rout[q] = r;
@@ -642,6 +657,26 @@ int mixed_alloc(nsmp_ctx* c) {
             l4[4 * k + j] = f[j];
         }
     }
+    // double-float splits v = hi + lo of the FP64 coefficients (the values the
+    // FP64 operator uses), hi = fl32(v), lo = fl32(v - hi)
+    auto split = [](double v, float* out) {
+        out[0] = (float)v;
+        out[1] = (float)(v - (double)out[0]);
+    };
+    std::vector<float> dc(8 * (size_t)L.N0, 0.f), dl(8 * (size_t)L.NZ, 0.f);
+    for (int q = 0; q < L.N0; ++q) {
+        for (int j = 0; j < 3; ++j) split(L.ppe[q].kA[j], &dc[8 * (size_t)q + 2 * j]);
+        split(L.ppe[q].area, &dc[8 * (size_t)q + 6]);
+    }
+    for (int k = 0; k < L.NZ; ++k) {
+        split(L.lev.dsv[k], &dl[8 * (size_t)k]);
+        split(L.lev.idsT[k] * L.lev.wT[k], &dl[8 * (size_t)k + 2]);
+        split(L.lev.idsB[k] * L.lev.wB[k], &dl[8 * (size_t)k + 4]);
+    }
+    CK(dalloc((void**)&c->ddcol, sizeof(float) * dc.size()));
+    CK(dalloc((void**)&c->ddlev, sizeof(float) * dl.size()));
+    CK(cudaMemcpyAsync(c->ddcol, dc.data(), sizeof(float) * dc.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->ddlev, dl.data(), sizeof(float) * dl.size(), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->d_ppe32, p32.data(), sizeof(ColPPE32) * L.N0, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->lev32, lv.data(), sizeof(float) * lv.size(), cudaMemcpyHostToDevice, c->stream));
     k_mix_setup<<<grid_for(c, (long long)ncf), kBlock, 0, c->stream>>>(c->mesh, c->invD, c->invD32);
@@ -714,7 +749,8 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     const int g_sc = grid_occ(c, k_mix_scale, m.nprism), g_sh = grid_occ(c, k_mix_shadow, m.nprism);
     MixArgs a{c->rhsp, pf, c->b64, c->r, c->x, c->xa, c->xb, c->r32, c->r032, c->p32[0], c->p32[1], c->v32[0],
               c->v32[1], c->s32, c->t32, c->e32, c->invD32, c->d_ppe32, c->lev32,
-              (m.NZI + 3) / 4 * 4, reinterpret_cast<const float4*>(c->lev32 + 3 * ((m.NZI + 3) / 4 * 4))};
+              (m.NZI + 3) / 4 * 4, reinterpret_cast<const float4*>(c->lev32 + 3 * ((m.NZI + 3) / 4 * 4)),
+              reinterpret_cast<const float4*>(c->ddcol), reinterpret_cast<const float4*>(c->ddlev)};
     CK(cudaMemcpyAsync(&c->d_scal->inner_tol, &c->inner_tol, sizeof(double), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(&c->d_scal->inner_cap, &c->inner_cap, sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(&c->d_scal->restart_every, &c->restart_every, sizeof(int), cudaMemcpyHostToDevice, st));
