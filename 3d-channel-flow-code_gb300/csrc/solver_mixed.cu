@@ -13,7 +13,7 @@
 //     x1 = x + e, r1 = b - A x1         FP64                 k_mix_update
 //     x, r <- x + theta (x1 - x), r + theta (r1 - r) with the minimal-residual
 //     theta; stopping test on the FP64 norms               k_mix_scale
-//     FP32 r <- r (true residual)       Krylov state kept   k_mix_scale/_shadow
+//     FP32 r <- r (true residual)       Krylov state kept   k_mix_scale
 //
 // Replacing the drifting FP32 recursive residual by the FP64 truth, while
 // keeping p, v, the shadow residual and rho, lets one Krylov process run to
@@ -537,7 +537,13 @@ __global__ void __launch_bounds__(kBlock) k_mix_scale(Mesh m, MixArgs a, RedScra
     // taken from its FP32 image r = iscale (rf + rm / iscale), to FP32
     // accuracy, so the pass costs three FP64 instructions a prism
     const float rmi = (float)(rm * inv);
-    float part[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    // the shadow residual of the next FP32 cycle and rho = (r0, r) are formed
+    // in the same pass; they take effect only if no check of b - A x is
+    // pending (see the end), and a pending check rewrites them from the
+    // checked residual before the next FP32 iteration
+    const int rst = sc->restart, jit = sc->perturb;
+    const unsigned int salt = (unsigned int)sc->outer;
+    float part[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
         double r = rn[g];
         if (blend) {
@@ -546,8 +552,19 @@ __global__ void __launch_bounds__(kBlock) k_mix_scale(Mesh m, MixArgs a, RedScra
             xn[g] = fma(th, xn[g] - xo[g], xo[g]);
         }
         const float rf = (float)((r - rm) * inv);
-        a.r[g] = rf * a.invD[g];  // r~ = D^-1 r
+        const float id = a.invD[g];
+        const float rt = rf * id;  // r~ = D^-1 r
+        a.r[g] = rt;
         a.e[g] = 0.f;
+        if (rst) {  // restart: r^0 = D r0 with r0 = r, perturbed after a stalled cycle
+            const float d = __frcp_rn(id);
+            const float ru = rt * d;
+            const float q0 = jit ? ru * (1.0f + 0.5f * shadow_jitter((unsigned int)g, salt)) : ru;
+            a.r0[g] = q0 * d;
+            part[5] = fmaf(q0, ru, part[5]);
+        } else {
+            part[5] = fmaf(a.r0[g], rt, part[5]);  // (r0, r) = (r^0, r~)
+        }
         const float ra = rf + rmi;
         part[0] += fabsf(ra);
         part[1] = fmaf(ra, ra, part[1]);
@@ -555,8 +572,8 @@ __global__ void __launch_bounds__(kBlock) k_mix_scale(Mesh m, MixArgs a, RedScra
         part[3] += fabsf(rf);
         part[4] = fmaf(rf, rf, part[4]);
     }
-    double tot[5];
-    if (grid_reduce_f<5>(part, rs, tot) && threadIdx.x == 0) {
+    double tot[6];
+    if (grid_reduce_f<6>(part, rs, tot) && threadIdx.x == 0) {
         const double is = sc->iscale;
         const double r1 = is * tot[0], r2 = is * sqrt(tot[1]);
         const int k = (sc->outer - 1) % Scal::kCycLog;
@@ -579,32 +596,13 @@ __global__ void __launch_bounds__(kBlock) k_mix_scale(Mesh m, MixArgs a, RedScra
         else if (sc->iter > sc->max_iters) { sc->status = NSMP_WARN_MAXITER; sc->done = 1; }
         else if (sc->outer >= 2000) { sc->status = NSMP_WARN_BREAKDOWN; sc->done = 1; }
         if (!(en < sc->eps)) sc->verify = 0;
-    }
-}
-
-// Shadow residual and rho for the next FP32 cycle (after k_mix_scale).
-__global__ void __launch_bounds__(kBlock) k_mix_shadow(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
-    if (sc->done || !sc->pending || sc->verify) return;  // a check of b - A x is pending
-    const int rst = sc->restart, jit = sc->perturb;
-    const unsigned int salt = (unsigned int)sc->outer;
-    double part[1] = {0.0};
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
-        const float rt = a.r[g];  // r~ = D^-1 r
-        if (rst) {
-            const float d = __frcp_rn(a.invD[g]);
-            const float rf = rt * d;  // r
-            const float q0 = jit ? rf * (1.0f + 0.5f * shadow_jitter((unsigned int)g, salt)) : rf;
-            a.r0[g] = q0 * d;  // r^0 = D r0
-            part[0] += (double)q0 * (double)rf;
-        } else {
-            part[0] += (double)a.r0[g] * (double)rt;  // (r0, r) = (r^0, r~)
+        // the next FP32 cycle starts from this residual unless the solve
+        // ended or a check of b - A x is pending
+        if (!sc->done && !sc->verify) {
+            sc->irho = tot[5];
+            if (rst) { sc->irho_prev = 1.0; sc->ialpha = 1.0; sc->iomega = 1.0; sc->iiter = 0; }
+            sc->ksince = 0; sc->pending = 0; sc->restart = 0; sc->perturb = 0; sc->rfresh = 1; sc->einc = 0;
         }
-    }
-    double tot[1];
-    if (grid_reduce<1, false>(part, rs, tot) && threadIdx.x == 0) {
-        sc->irho = tot[0];
-        if (rst) { sc->irho_prev = 1.0; sc->ialpha = 1.0; sc->iomega = 1.0; sc->iiter = 0; }
-        sc->ksince = 0; sc->pending = 0; sc->restart = 0; sc->perturb = 0; sc->rfresh = 1; sc->einc = 0;
     }
 }
 
@@ -746,7 +744,7 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     const int g_pv = quad ? grid_occ(c, k_in_pv<4>, m.nprism / L) : grid_occ(c, k_in_pv<2>, m.nprism / L);
     const int g_st = quad ? grid_occ(c, k_in_st<4>, m.nprism / L) : grid_occ(c, k_in_st<2>, m.nprism / L);
     const int g_in = grid_occ(c, k_mix_init, m.nprism), g_u = grid_occ(c, k_mix_update, m.nprism);
-    const int g_sc = grid_occ(c, k_mix_scale, m.nprism), g_sh = grid_occ(c, k_mix_shadow, m.nprism);
+    const int g_sc = grid_occ(c, k_mix_scale, m.nprism);
     MixArgs a{c->rhsp, pf, c->b64, c->r, c->x, c->xa, c->xb, c->r32, c->r032, c->p32[0], c->p32[1], c->v32[0],
               c->v32[1], c->s32, c->t32, c->e32, c->invD32, c->d_ppe32, c->lev32,
               (m.NZI + 3) / 4 * 4, reinterpret_cast<const float4*>(c->lev32 + 3 * ((m.NZI + 3) / 4 * 4)),
@@ -757,7 +755,6 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     LAUNCH(NSMP_K_BICG_INIT, k_mix_init<<<g_in, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
     LAUNCH(NSMP_K_MIX_UPDATE, k_mix_update<<<g_u, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
     LAUNCH(NSMP_K_MIX_SCALE, k_mix_scale<<<g_sc, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-    LAUNCH(NSMP_K_MIX_SCALE, k_mix_shadow<<<g_sh, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
     CKL("k_mix_init");
     // FP32 iterations in chunks, an FP64 update slot after every few
     // iterations (it only acts when one was requested); the host polls for
@@ -778,7 +775,6 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
             }
             LAUNCH(NSMP_K_MIX_UPDATE, k_mix_update<<<g_u, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
             LAUNCH(NSMP_K_MIX_SCALE, k_mix_scale<<<g_sc, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-            LAUNCH(NSMP_K_MIX_SCALE, k_mix_shadow<<<g_sh, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
         }
         CKL("mixed inner chunk");
         launched += chunk;
