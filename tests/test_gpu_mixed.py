@@ -33,6 +33,27 @@ def test_mixed_one_stage_vs_oracle():
     assert rel_l2(interior(s.download(ng.F_P), o.n0), interior(o.get(oc.F_P), o.n0)) <= 1e-9
 
 
+def test_incremental_residual_matches_recomputed():
+    """The hand-over's incremental residual r - s A (e - mean e), with A c in
+    double-float FP32, stays accurate.  A mixed solve is only declared
+    converged after an update that recomputes b - A x from scratch in FP64
+    for the same x, so the last two updates of a converged solve report the
+    incremental and the recomputed residual of one iterate.  Their norms
+    agree to 1 % at eps = 1e-10 (measured: to 5 digits; the double-float
+    drift bound is of order 1e-12 |b|); A c with FP32 accuracy would be off
+    by orders of magnitude."""
+    prm, mesh = small_case(32, 16, layers=32, dt=1e-3, eps=1e-10, max_iters=20000, precision=ng.MIXED)
+    s, _ = _start(prm, mesh)
+    for _ in range(3):  # three Euler/AB2 stages, each with its own solve
+        rc, inf = s.step(1, 1)
+        assert rc == 0 and inf["converged"] == 1
+        log = s.solver_log()
+        assert len(log) >= 3, log
+        inc, rec = log[-2][2], log[-1][2]
+        assert rec > 0.0 and abs(inc - rec) <= 0.01 * rec, (inc, rec)
+    s.close()
+
+
 def test_mixed_matches_fp64_after_steps():
     """configs[0] mesh, 20 RK3 steps at eps = 1e-10: mixed vs FP64 GPU."""
     prm, mesh = small_case(32, 16, layers=32, dt=1e-3)
