@@ -76,6 +76,26 @@ int nsmp_ncell(const nsmp_ctx* c, int* n_cell) {
 
 void* nsmp_stream(nsmp_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
+int nsmp_host_register(nsmp_ctx* c, void* host, size_t bytes) {
+    if (!c || !host || bytes == 0) return NSMP_ERR_ARG;
+    const cudaError_t e = cudaHostRegister(host, bytes, cudaHostRegisterPortable);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(c, NSMP_ERR_CUDA, std::string("nsmp_host_register: ") + cudaGetErrorString(e));
+    }
+    return NSMP_OK;
+}
+
+int nsmp_host_unregister(nsmp_ctx* c, void* host) {
+    if (!c || !host) return NSMP_ERR_ARG;
+    const cudaError_t e = cudaHostUnregister(host);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(c, NSMP_ERR_CUDA, std::string("nsmp_host_unregister: ") + cudaGetErrorString(e));
+    }
+    return NSMP_OK;
+}
+
 int nsmp_user_initial(nsmp_ctx* c, const double* u, const double* v, const double* w, const double* p) {
     if (!c || !u || !v || !w || !p) return NSMP_ERR_ARG;
     const double* in[4] = {u, v, w, p};

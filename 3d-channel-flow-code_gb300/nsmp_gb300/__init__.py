@@ -59,7 +59,8 @@ EXPORTS = [
     "nsmp_create", "nsmp_destroy", "nsmp_last_error", "nsmp_ncell", "nsmp_user_initial", "nsmp_upload_state",
     "nsmp_download", "nsmp_copy_known_from_n", "nsmp_hydro_stage", "nsmp_copy_known_from_np",
     "nsmp_rk2_finalize", "nsmp_rk_combine", "nsmp_time_update", "nsmp_step", "nsmp_mass_diag",
-    "nsmp_set_precision", "nsmp_stream", "nsmp_mesh_size", "nsmp_mesh_generate", "nsmp_initial_channel",
+    "nsmp_set_precision", "nsmp_stream", "nsmp_host_register", "nsmp_host_unregister", "nsmp_mesh_size",
+    "nsmp_mesh_generate", "nsmp_initial_channel",
     "nsmp_sigma_grid", "nsmp_geometry", "nsmp_prof_enable", "nsmp_prof_read", "nsmp_counters",
     "nsmp_set_inner_solver", "nsmp_solver_log", "nsmp_mass_diag_noalloc",
     "nsmp_set_body_force", "nsmp_wall_shear", "nsmp_adjoint", "nsmp_apply_A", "nsmp_apply_AT",
@@ -126,6 +127,8 @@ def lib(build_if_missing=True):
     L.nsmp_apply_AT.argtypes = [vp, vp, vp]
     L.nsmp_stream.argtypes = [vp]
     L.nsmp_stream.restype = vp
+    L.nsmp_host_register.argtypes = [vp, vp, C.c_size_t]
+    L.nsmp_host_unregister.argtypes = [vp, vp]
     L.nsmp_mesh_size.argtypes = [C.c_int, C.c_int, P(C.c_int), P(C.c_int)]
     L.nsmp_mesh_generate.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                      C.c_double, C.c_ulonglong] + [vp] * 6
@@ -270,6 +273,14 @@ class Solver:
         arrs = [np.asfortranarray(a, dtype=np.float64) for a in [u, v, w, p] + list(faces) + list(hist)]
         self._check(self.L.nsmp_upload_state(self.h, *[_p(a) for a in arrs], int(flag_ab)))
         self.flag_ab = int(flag_ab)
+
+    def host_register(self, arr):
+        """Page-lock a host array (nsmp_host_register) so uploads and
+        downloads through it are direct copies."""
+        self._check(self.L.nsmp_host_register(self.h, arr.ctypes.data, arr.nbytes))
+
+    def host_unregister(self, arr):
+        self._check(self.L.nsmp_host_unregister(self.h, arr.ctypes.data))
 
     def download(self, field, out=None):
         """Field in the reference's Fortran layout; into `out` (float64,

@@ -120,6 +120,15 @@ int nsmp_upload_state(nsmp_ctx* ctx, const double* u, const double* v,
                       const double* ubf, const double* rhsu, const double* rhsv,
                       const double* rhsw, int flag_ab);
 int nsmp_download(nsmp_ctx* ctx, int field, double* host);
+/* Optional: page-lock (cudaHostRegister, portable) a host array that the
+ * driver passes to the uploads and downloads above, so their copies run as
+ * direct DMA instead of through the CUDA driver's pageable staging buffer;
+ * nsmp_host_unregister undoes it before the array is deallocated.  Both are
+ * host-memory bookkeeping only: results are the same either way.  Uploads
+ * return after their copies have completed and downloads after the data has
+ * arrived, so registered or not, an array may be reused at once. */
+int nsmp_host_register(nsmp_ctx* ctx, void* host, size_t bytes);
+int nsmp_host_unregister(nsmp_ctx* ctx, void* host);
 
 /* ---- time loop: nsmp3D.F90:394-564 ------------------------------------ */
 

@@ -210,6 +210,32 @@ def test_upload_download_roundtrip_is_exact():
     s.close()
 
 
+def test_host_registered_arrays_roundtrip():
+    """nsmp_host_register page-locks the driver's own arrays; uploads and
+    downloads through them give the same bits as through ordinary memory."""
+    prm, mesh = small_case(8, 6, layers=6)
+    s = ng.Solver(prm, mesh)
+    rng = np.random.default_rng(12)
+    n0, nc, nz = prm["n0"], s.ncell, s.nz
+    cells = [np.asfortranarray(rng.standard_normal((nc, nz))) for _ in range(4)]
+    faces = [np.asfortranarray(rng.standard_normal((n0, nz))) for _ in range(5)]
+    hist = [np.asfortranarray(rng.standard_normal((nc, nz))) for _ in range(3)]
+    outs = [np.zeros((nc, nz), order="F") for _ in range(4)]
+    arrays = cells + faces + hist + outs
+    for a in arrays:
+        s.host_register(a)
+    s.upload_state(*cells, faces, hist, 1)
+    s.step(3, 1)
+    for o, f in zip(outs, (ng.F_U, ng.F_V, ng.F_W, ng.F_P)):
+        s.download(f, out=o)
+        assert np.array_equal(o, s.download(f))
+    for a in arrays:
+        s.host_unregister(a)
+    with pytest.raises(ng.NsmpError):
+        s.host_unregister(outs[0])  # no longer registered
+    s.close()
+
+
 @pytest.mark.slow
 def test_config0_100_steps():
     """configs[0]: 100 RK3 steps, relative L2 <= 1e-8 per field."""
