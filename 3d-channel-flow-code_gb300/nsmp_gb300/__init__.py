@@ -168,7 +168,7 @@ def make_mesh(nx, ny, lx=2 * PI_REF, ly=PI_REF, jitter=0.2, seed=0):
 def channel_params(nx, ny, layers, dt, lx=2 * PI_REF, ly=PI_REF, height=2.0, re=180.0, les=1, les_van=1,
                    grid_kind=1, beta=2.0, eps=1e-10, max_iters=10000, top_bc=0, bot_bc=0, ref_bug_compat=1,
                    precision=FP64, device=0):
-    """Parameter dict of the periodic channel (BASELINE geometry by default)."""
+    """Parameter dict of the periodic channel (2pi x pi x 2, tanh layers, dp/dx = -1 by default)."""
     return dict(n0=2 * nx * ny, nvert=(nx + 1) * (ny + 1), nz=layers + 2, xdini=0.0, xdfin=lx, ydini=0.0,
                 ydfin=ly, sigini=0.0, sigfin=height, grid_kind=grid_kind, grid_beta=beta, top_bc=top_bc,
                 bot_bc=bot_bc, dt=dt, re=re, bdx=1.0, bdy=0.0, bdz=0.0, eps=eps, max_iters=max_iters, les=les,

@@ -55,7 +55,7 @@ def test_incremental_residual_matches_recomputed():
 
 
 def test_mixed_matches_fp64_after_steps():
-    """configs[0] mesh, 20 RK3 steps at eps = 1e-10: mixed vs FP64 GPU."""
+    """32,768-prism mesh, 20 RK3 steps at eps = 1e-10: mixed vs FP64 GPU."""
     prm, mesh = small_case(32, 16, layers=32, dt=1e-3)
     s64, _ = _start(prm, mesh)
     s32, _ = _start(dict(prm, precision=ng.MIXED), mesh)

@@ -11,7 +11,7 @@ What is pinned, and how:
     seed), so at the reference tolerance 1e-10 iteration counts agree within
     a band (25 %), not +-1, and fields agree to the solver tolerance;
   * time integration -- Euler->AB2, RK2 and RK3 over several steps, and
-    100 RK3 steps of configs[0] at relative L2 <= 1e-8.
+    100 RK3 steps of the 32,768-prism case at relative L2 <= 1e-8.
 """
 import numpy as np
 import pytest
@@ -106,7 +106,7 @@ def test_one_stage_at_reference_tolerance():
 
 
 def test_config0_one_step_rk3():
-    """configs[0] geometry: 32x16 quads, 32 tanh layers, RK3, dt = 1e-3."""
+    """The 32,768-prism case: 32x16 quads, 32 tanh layers, RK3, dt = 1e-3."""
     prm, mesh = small_case(32, 16, layers=32, dt=1e-3, eps=TIGHT, max_iters=3000)
     o, s = _pair(prm, mesh)
     o.step(3)
@@ -238,7 +238,7 @@ def test_host_registered_arrays_roundtrip():
 
 @pytest.mark.slow
 def test_config0_100_steps():
-    """configs[0]: 100 RK3 steps, relative L2 <= 1e-8 per field."""
+    """The 32,768-prism case: 100 RK3 steps, relative L2 <= 1e-8 per field."""
     prm, mesh = small_case(32, 16, layers=32, dt=1e-3, eps=1e-13, max_iters=3000)
     o, s = _pair(prm, mesh)
     for _ in range(100):
