@@ -168,6 +168,18 @@ __device__ bool grid_reduce(double (&x)[N], RedScratch rs, double (&tot)[N]) {
     return grid_finish<N, MAX>(x, rs, tot);
 }
 
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialization (launch_pdl) may be scheduled while its predecessor in the
+// stream drains; it waits here until the predecessor has completed and its
+// memory is visible, then releases its own dependent launch.  A dependent
+// grid is launched only after every block of its predecessor has started, so
+// its waiting blocks never hold back a block of the predecessor.  Both
+// instructions are no-ops for an ordinary launch.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Double-float arithmetic: a value is an unevaluated sum h + l of two FP32
 // numbers with |l| <= ulp(h)/2, about 48 significant bits.  The algorithms
 // are the published error-free transformations: TwoSum (Knuth, TAOCP vol. 2),

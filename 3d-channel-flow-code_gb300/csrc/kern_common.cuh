@@ -1,6 +1,8 @@
 // Helpers shared by the kernel translation units: prism indexing, the
 // FP64 PPE row, grid sizing and the launch/error macros.
 #pragma once
+#include <utility>
+
 #include "ctx.h"
 
 namespace nsmp {
@@ -43,6 +45,22 @@ inline int grid_for(const nsmp_ctx* c, long long n) {
     return (int)b;
 }
 
+// Launch with programmatic stream serialization: the kernel may start while
+// the previous kernel of the stream drains, and must begin with pdl_enter().
+template <typename... P, typename... A>
+cudaError_t launch_pdl(void (*kernel)(P...), int grid, cudaStream_t st, A&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)kBlock);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
 
 }  // namespace nsmp
 

@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(kBlock) k_bicg_init(Mesh m, KryArgs a, RedScra
 
 // update_pk (bicgstab.F90:726-773), two prisms per thread.
 __global__ void __launch_bounds__(kBlock) k_bicg_p(Mesh m, KryArgs a, const Scal* sc) {
+    pdl_enter();
     if (sc->done) return;
     const int it = sc->iter;
     const double beta = (sc->rho / sc->rho_prev) * (sc->alpha / sc->omega), om = sc->omega;
@@ -113,6 +114,7 @@ __global__ void __launch_bounds__(kBlock) k_bicg_p(Mesh m, KryArgs a, const Scal
 // fused dots.  MODE 0: v = A D^-1 p, (r0, v);  MODE 1: t = A D^-1 s, (t, s), (t, t).
 template <int MODE>
 __global__ void __launch_bounds__(kBlock) k_bicg_spmv(Mesh m, KryArgs a, RedScratch rs, Scal* sc) {
+    pdl_enter();
     if (sc->done) return;
     const double* __restrict__ in = (MODE == 0) ? a.p : a.s;
     double* __restrict__ out = (MODE == 0) ? a.v : a.t;
@@ -157,6 +159,7 @@ __global__ void __launch_bounds__(kBlock) k_bicg_spmv(Mesh m, KryArgs a, RedScra
 
 // update_sk (bicgstab.F90:1007-1041)
 __global__ void __launch_bounds__(kBlock) k_bicg_s(Mesh m, KryArgs a, const Scal* sc) {
+    pdl_enter();
     if (sc->done) return;
     const double al = sc->alpha;
     const int n2 = m.nprism >> 1;
@@ -185,6 +188,7 @@ __device__ __forceinline__ void xr_one(double id, double al, double om, double p
 }
 
 __global__ void __launch_bounds__(kBlock) k_bicg_x(Mesh m, KryArgs a, RedScratch rs, Scal* sc) {
+    pdl_enter();
     if (sc->done) return;
     const double al = sc->alpha, om = sc->omega;
     double part[3] = {0.0, 0.0, 0.0};
@@ -263,11 +267,11 @@ int run_pressure_fp64(nsmp_ctx* c, const double* pf, const double** x_final) {
     int launched = 0;
     for (;;) {
         for (int it = 0; it < chunk; ++it) {
-            LAUNCH(NSMP_K_BICG_P, k_bicg_p<<<g_p, kBlock, 0, st>>>(m, ka, c->d_scal));
-            LAUNCH(NSMP_K_BICG_SPMV_V, k_bicg_spmv<0><<<g_v, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
-            LAUNCH(NSMP_K_BICG_S, k_bicg_s<<<g_s, kBlock, 0, st>>>(m, ka, c->d_scal));
-            LAUNCH(NSMP_K_BICG_SPMV_T, k_bicg_spmv<1><<<g_t, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
-            LAUNCH(NSMP_K_BICG_X, k_bicg_x<<<g_x, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
+            LAUNCH(NSMP_K_BICG_P, CK(launch_pdl(k_bicg_p, g_p, st, m, ka, c->d_scal)));
+            LAUNCH(NSMP_K_BICG_SPMV_V, CK(launch_pdl(k_bicg_spmv<0>, g_v, st, m, ka, c->red, c->d_scal)));
+            LAUNCH(NSMP_K_BICG_S, CK(launch_pdl(k_bicg_s, g_s, st, m, ka, c->d_scal)));
+            LAUNCH(NSMP_K_BICG_SPMV_T, CK(launch_pdl(k_bicg_spmv<1>, g_t, st, m, ka, c->red, c->d_scal)));
+            LAUNCH(NSMP_K_BICG_X, CK(launch_pdl(k_bicg_x, g_x, st, m, ka, c->red, c->d_scal)));
         }
         CKL("bicgstab iteration");
         launched += chunk;

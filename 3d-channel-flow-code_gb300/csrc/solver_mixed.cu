@@ -279,6 +279,7 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
 // (8 % faster at 6.3M prisms).
 template <int L>
 __global__ void __launch_bounds__(kBlock, 4) k_in_pv(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
+    pdl_enter();
     if (sc->done || sc->pending) return;
     const int it = sc->iiter;
     const int mode = (it == 0) ? 0 : (sc->rfresh ? 1 : 2);
@@ -320,6 +321,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_in_pv(Mesh m, MixArgs a, RedScrat
 // parallel to s, as it is for smooth residuals.
 template <int L>
 __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
+    pdl_enter();
     if (sc->done || sc->pending) return;
     const int it = sc->iiter, NZI = m.NZI;
     const float al = (float)sc->ialpha;
@@ -417,6 +419,7 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
 // dropping the correction and restarting from the same residual would retrace
 // the same FP32 iterations, deterministically, forever.)
 __global__ void __launch_bounds__(kBlock) k_mix_update(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
+    pdl_enter();
     if (sc->done || !sc->pending) return;
     const int cur = sc->cur;
     const int has_e = sc->has_e;
@@ -524,6 +527,7 @@ __device__ __forceinline__ float shadow_jitter(unsigned int g, unsigned int k) {
 // is measured against and rho = (r0, r).  On a restart also r0 = r and a
 // fresh Krylov process.
 __global__ void __launch_bounds__(kBlock) k_mix_scale(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
+    pdl_enter();
     if (sc->done || !sc->pending) return;
     const int cur = sc->cur;
     const double th = sc->theta;
@@ -753,8 +757,8 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     CK(cudaMemcpyAsync(&c->d_scal->inner_cap, &c->inner_cap, sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(&c->d_scal->restart_every, &c->restart_every, sizeof(int), cudaMemcpyHostToDevice, st));
     LAUNCH(NSMP_K_BICG_INIT, k_mix_init<<<g_in, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-    LAUNCH(NSMP_K_MIX_UPDATE, k_mix_update<<<g_u, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-    LAUNCH(NSMP_K_MIX_SCALE, k_mix_scale<<<g_sc, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+    LAUNCH(NSMP_K_MIX_UPDATE, CK(launch_pdl(k_mix_update, g_u, st, m, a, c->red, c->d_scal)));
+    LAUNCH(NSMP_K_MIX_SCALE, CK(launch_pdl(k_mix_scale, g_sc, st, m, a, c->red, c->d_scal)));
     CKL("k_mix_init");
     // FP32 iterations in chunks, an FP64 update slot after every few
     // iterations (it only acts when one was requested); the host polls for
@@ -766,15 +770,15 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
         for (int it = 0; it < chunk; it += per_update) {
             for (int j = 0; j < per_update; ++j) {
                 if (quad) {
-                    LAUNCH(NSMP_K_IN_PV, k_in_pv<4><<<g_pv, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-                    LAUNCH(NSMP_K_IN_ST, k_in_st<4><<<g_st, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+                    LAUNCH(NSMP_K_IN_PV, CK(launch_pdl(k_in_pv<4>, g_pv, st, m, a, c->red, c->d_scal)));
+                    LAUNCH(NSMP_K_IN_ST, CK(launch_pdl(k_in_st<4>, g_st, st, m, a, c->red, c->d_scal)));
                 } else {
-                    LAUNCH(NSMP_K_IN_PV, k_in_pv<2><<<g_pv, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-                    LAUNCH(NSMP_K_IN_ST, k_in_st<2><<<g_st, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+                    LAUNCH(NSMP_K_IN_PV, CK(launch_pdl(k_in_pv<2>, g_pv, st, m, a, c->red, c->d_scal)));
+                    LAUNCH(NSMP_K_IN_ST, CK(launch_pdl(k_in_st<2>, g_st, st, m, a, c->red, c->d_scal)));
                 }
             }
-            LAUNCH(NSMP_K_MIX_UPDATE, k_mix_update<<<g_u, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
-            LAUNCH(NSMP_K_MIX_SCALE, k_mix_scale<<<g_sc, kBlock, 0, st>>>(m, a, c->red, c->d_scal));
+            LAUNCH(NSMP_K_MIX_UPDATE, CK(launch_pdl(k_mix_update, g_u, st, m, a, c->red, c->d_scal)));
+            LAUNCH(NSMP_K_MIX_SCALE, CK(launch_pdl(k_mix_scale, g_sc, st, m, a, c->red, c->d_scal)));
         }
         CKL("mixed inner chunk");
         launched += chunk;
