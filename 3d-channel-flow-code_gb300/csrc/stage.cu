@@ -337,24 +337,49 @@ __global__ void k_combine(size_t n, double a, double b, const double* __restrict
 
 // (N_CELL,NZ) Fortran order <-> device columns.  ghost_mode 0: ghost rows
 // copy the periodic image; 1: ghost rows are 0.
-__global__ void k_gather(int ncell, int nz, int layers, int kofs, const int* __restrict__ col,
-                         const double* __restrict__ f, int ghost_mode, int n0, double* __restrict__ out) {
-    const size_t n = (size_t)ncell * layers;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int cell = (int)(i % ncell), k = (int)(i / ncell);
-        double val = f[(size_t)col[cell] * nz + k + kofs];
-        if (ghost_mode == 1 && cell >= n0) val = 0.0;
-        out[i] = val;
+// Device columns <-> the reference's (rows, NZ) Fortran arrays.  The two
+// layouts are transposes of each other, so both directions go through a
+// 32 x 32 shared-memory tile: a column's layers are read (written)
+// contiguously on the device side and a layer's rows written (read)
+// contiguously on the host-array side.
+constexpr int kTile = 32, kTileRows = 8;  // tile edge, thread rows of a block
+
+// out(cell, k) = f(col[cell], k + kofs) for cell < ncell, k < layers; rows
+// cell >= n0 are zero when ghost_mode = 1.
+__global__ void __launch_bounds__(kTile * kTileRows) k_gather(int ncell, int nz, int layers, int kofs,
+                                                             const int* __restrict__ col,
+                                                             const double* __restrict__ f, int ghost_mode, int n0,
+                                                             double* __restrict__ out) {
+    __shared__ double tile[kTile][kTile + 1];
+    const int c0 = blockIdx.x * kTile, k0 = blockIdx.y * kTile, tx = threadIdx.x;
+    for (int j = threadIdx.y; j < kTile; j += kTileRows) {
+        const int cell = c0 + j, k = k0 + tx;
+        if (cell < ncell && k < layers) {
+            const double v = f[(size_t)col[cell] * nz + k + kofs];
+            tile[j][tx] = (ghost_mode == 1 && cell >= n0) ? 0.0 : v;
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < kTile; j += kTileRows) {
+        const int cell = c0 + tx, k = k0 + j;
+        if (cell < ncell && k < layers) out[(size_t)cell + (size_t)k * ncell] = tile[tx][j];
     }
 }
 
-// in is a (rows,NZ) Fortran array; its first n0 rows go to the columns.
-__global__ void k_scatter(int n0, int nz, int rows, const int* __restrict__ col, const double* __restrict__ in,
-                          double* __restrict__ f) {
-    const size_t n = (size_t)n0 * nz;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int cell = (int)(i % n0), k = (int)(i / n0);
-        f[(size_t)col[cell] * nz + k] = in[(size_t)cell + (size_t)k * rows];
+// f(col[cell], k) = in(cell, k) for cell < n0, k < nz; in is (rows, nz).
+__global__ void __launch_bounds__(kTile * kTileRows) k_scatter(int n0, int nz, int rows, const int* __restrict__ col,
+                                                              const double* __restrict__ in,
+                                                              double* __restrict__ f) {
+    __shared__ double tile[kTile][kTile + 1];
+    const int c0 = blockIdx.x * kTile, k0 = blockIdx.y * kTile, tx = threadIdx.x;
+    for (int j = threadIdx.y; j < kTile; j += kTileRows) {
+        const int cell = c0 + tx, k = k0 + j;
+        if (cell < n0 && k < nz) tile[j][tx] = in[(size_t)cell + (size_t)k * rows];
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < kTile; j += kTileRows) {
+        const int cell = c0 + j, k = k0 + tx;
+        if (cell < n0 && k < nz) f[(size_t)col[cell] * nz + k] = tile[tx][j];
     }
 }
 
@@ -583,8 +608,9 @@ int run_gather(nsmp_ctx* c, const double* dfield, int ghost_mode, int rows, doub
     const int ncell = rows;
     const int layers = c->mesh.NZ;
     const size_t n = (size_t)ncell * layers;
-    k_gather<<<grid_for(c, (long long)n), kBlock, 0, c->stream>>>(ncell, c->mesh.NZ, layers, 0, c->d_gather,
-                                                                  dfield, ghost_mode, c->L.N0, c->stage_buf);
+    const dim3 tiles((ncell + kTile - 1) / kTile, (layers + kTile - 1) / kTile), tb(kTile, kTileRows);
+    k_gather<<<tiles, tb, 0, c->stream>>>(ncell, c->mesh.NZ, layers, 0, c->d_gather, dfield, ghost_mode, c->L.N0,
+                                          c->stage_buf);
     CKL("k_gather");
     CK(cudaMemcpyAsync(host, c->stage_buf, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -614,8 +640,8 @@ int run_scatter(nsmp_ctx* c, const double* host, double* dfield, int rows, bool 
         return NSMP_ERR_ARG;
     }
     CK(cudaMemcpyAsync(c->stage_buf, host, (size_t)rows * nz * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    k_scatter<<<grid_for(c, (long long)n0 * nz), kBlock, 0, c->stream>>>(n0, nz, rows, c->d_gather, c->stage_buf,
-                                                                         dfield);
+    const dim3 tiles((n0 + kTile - 1) / kTile, (nz + kTile - 1) / kTile), tb(kTile, kTileRows);
+    k_scatter<<<tiles, tb, 0, c->stream>>>(n0, nz, rows, c->d_gather, c->stage_buf, dfield);
     CKL("k_scatter");
     if (sync) CK(cudaStreamSynchronize(c->stream));
     return 0;
