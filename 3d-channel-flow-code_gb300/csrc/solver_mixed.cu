@@ -10,10 +10,13 @@
 //   FP32 BiCGSTAB iterations on A e = r, e accumulated     k_in_pv / k_in_st
 //   when the FP32 residual fell by inner_tol (or after
 //   inner_cap iterations):
-//     x1 = x + e, r1 = b - A x1         FP64                 k_mix_update
+//     x1 = x + e, r1 = r - A e           FP64 updates, A e   k_mix_update
+//                                        double-float FP32
 //     x, r <- x + theta (x1 - x), r + theta (r1 - r) with the minimal-residual
 //     theta; stopping test on the FP64 norms               k_mix_scale
 //     FP32 r <- r (true residual)       Krylov state kept   k_mix_scale
+//   convergence is declared only after an update that forms r1 = b - A x1
+//   from scratch in FP64 passes the test again.
 //
 // Replacing the drifting FP32 recursive residual by the FP64 truth, while
 // keeping p, v, the shadow residual and rho, lets one Krylov process run to
