@@ -210,11 +210,13 @@ def run_reference(args):
 # e and r0 read, p, v, r and e written (11 FP32 words; the pass after an FP64
 # update reads r instead of s and t and writes neither r nor e: 8).  k_in_st:
 # r, v, D^-1 (stencil) and r0 read, s and t written (6 FP32 words).
-# k_mix_update: x (FP64, stencil), e and the last increment's p, s, D^-1
-# (FP32), b read, x and r written.  k_mix_scale: FP64 r, D^-1 and r0 read,
+# k_mix_update (incremental form): FP64 x and r read, e and the last
+# increment's s and p (FP32, stencil) read, FP64 x and r written (5.5 words;
+# the from-scratch form on the first call reads b and x instead).
+# k_mix_scale: FP64 r, D^-1 and r0 read,
 # FP32 r and e written (r0 rewritten only on a Krylov restart).
 WORDS_MIXED = {
-    "k_in_pv": 11 * 0.5, "k_in_st": 6 * 0.5, "k_mix_update": 1 + 4 * 0.5 + 1 + 2, "k_mix_scale": 1 + 4 * 0.5,
+    "k_in_pv": 11 * 0.5, "k_in_st": 6 * 0.5, "k_mix_update": 1 + 1 + 3 * 0.5 + 2, "k_mix_scale": 1 + 4 * 0.5,
 }
 
 
