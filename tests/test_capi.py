@@ -32,6 +32,49 @@ def test_library_exports_header():
     assert set(ng.EXPORTS) <= set(names)
 
 
+def ctx_functions():
+    """Header functions whose first parameter is the context, with the C
+    types of their parameters."""
+    src = open(os.path.join(REPO, "include", "nsmp.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    out = []
+    for ret, name, params in re.findall(r"^\s*((?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\*?)\s*(nsmp_[A-Za-z0-9_]+)\s*\(([^)]*)\)\s*;",
+                                        src, flags=re.M):
+        ps = [p.strip() for p in params.replace("\n", " ").split(",")]
+        if ps and ps[0].startswith("nsmp_ctx"):
+            out.append((ret.strip(), name, ps))
+    return out
+
+
+def test_null_context_is_rejected_without_a_gpu():
+    """Every entry point that takes a context returns NSMP_ERR_ARG for a null
+    one (before touching CUDA, so this runs on a CPU); the pointer and string
+    queries return null and a message."""
+    L = ng.lib()
+    fns = ctx_functions()
+    assert len(fns) >= 30
+    for ret, name, ps in fns:
+        f = getattr(L, name)
+        typed = f.argtypes is not None  # else wrap values in their ctypes types
+        args = []
+        for p in ps[1:]:
+            if "*" in p or "[" in p:
+                args.append(None)
+            elif p.startswith("double"):
+                args.append(0.5 if typed else C.c_double(0.5))
+            elif p.startswith("size_t"):
+                args.append(1 if typed else C.c_size_t(1))
+            else:
+                args.append(1 if typed else C.c_int(1))
+        rv = f(None, *args)
+        if name == "nsmp_stream":
+            assert rv is None
+        elif name == "nsmp_last_error":
+            assert rv == b"null context"
+        else:
+            assert rv == -1, (name, rv)  # NSMP_ERR_ARG
+
+
 def header_enum(first):
     """Names of the C enum whose first member is `first`, in order."""
     src = open(os.path.join(REPO, "include", "nsmp.h")).read()
