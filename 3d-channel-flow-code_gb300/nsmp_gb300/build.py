@@ -23,8 +23,14 @@ LIB = os.path.join(LIBDIR, "libnsmpgpu.so")
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", "-I", INCLUDE, "-I", CSRC]
-NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
+# Host code is built without floating-point contraction (GCC fuses a*b+c by
+# default in C++ on targets with FMA, such as aarch64 but not baseline
+# x86-64), so the setup gives the same bits on every host and matches the
+# oracle, which is built the same way.
+CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", "-I", INCLUDE,
+            "-I", CSRC]
+NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+                  "-I", INCLUDE, "-I", CSRC,
                   "--expt-relaxed-constexpr"]
 
 
