@@ -1,0 +1,41 @@
+"""Host-side arithmetic of the benchmark: the whole-job metric and the
+roofline of the dominant kernel, from a synthetic per-kernel profile (no GPU
+needed)."""
+import math
+
+import bench
+
+
+def test_job_value_is_whole_job_throughput():
+    # 2 replicas x 6,291,456 prisms x 5 steps in 2 s -> 31.5 Mcell-steps/s
+    assert math.isclose(bench.job_value(2, 6291456, 5, 2000.0), 2 * 6291456 * 5 / 2.0 / 1e6)
+
+
+def test_roofline_of_the_mixed_solver():
+    prisms, iters = 6291456, 1000
+    # k_in_pv: 1000 busy launches plus idle slots, 67 ms in total
+    prof = {"k_in_pv": (1100, 67.0), "k_in_st": (1100, 40.0), "k_mix_update": (30, 4.0), "k_stage_rhs": (3, 7.0)}
+    roof, shares, total = bench.roofline(prof, iters, prisms, mixed=True)
+    peak, kind = bench.load_peaks()
+    assert roof["kernel"] == "k_in_pv" and roof["bound"] == "hbm" and roof["unit"] == "GB/s"
+    # algorithmic bytes: 11 FP32 words a prism, counted per busy iteration
+    bpl = 11 * 4 * prisms
+    assert roof["algorithmic_bytes_per_launch"] == bpl
+    achieved = bpl * iters / 0.067 / 1e9
+    assert math.isclose(roof["achieved"], round(achieved, 1))
+    assert math.isclose(roof["frac"], round(achieved / peak, 4))
+    assert roof["peak"] == peak and roof["peak_kind"] == kind
+    assert math.isclose(roof["avg_launch_ms"], 67.0 / iters)
+    assert math.isclose(total, 118.0)
+    assert math.isclose(sum(shares.values()), 1.0, abs_tol=1e-3)
+    assert roof["fp64_tflops"] is None  # FP32 kernel
+
+
+def test_roofline_of_the_fp64_solver_reports_its_fp64_rate():
+    prisms, iters = 1048576, 500
+    prof = {"k_bicg_x": (500, 17.5), "k_bicg_p": (500, 5.0)}
+    roof, _, _ = bench.roofline(prof, iters, prisms, mixed=False)
+    assert roof["kernel"] == "k_bicg_x"
+    assert roof["algorithmic_bytes_per_launch"] == 8 * 8 * prisms
+    flops = bench.FLOPS["k_bicg_x"] * prisms * iters
+    assert math.isclose(roof["fp64_tflops"], round(flops / 0.0175 / 1e12, 3))
