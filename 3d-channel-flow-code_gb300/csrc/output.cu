@@ -25,24 +25,40 @@ __device__ __forceinline__ double class_idw(const Mesh& m, const double* __restr
     return a;
 }
 
-// out[nv + kv * nvert], kv = 0..NZ-2 (reference vertex layer kv+1)
-__global__ void k_vertex_out(Mesh m, int nvert, const int* __restrict__ vcls, const double* __restrict__ f,
-                             int tagdir, const double* __restrict__ wT, const double* __restrict__ wB,
-                             int zero_bot, int zero_top, double* __restrict__ out) {
-    const size_t n = (size_t)nvert * (m.NZ - 1);
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int nv = (int)(i % nvert), kv = (int)(i / nvert);
-        const int v = vcls[nv];
-        double val;
-        if (tagdir == 2) {
-            val = class_idw(m, f, v, kv);
-        } else if ((kv == 0 && zero_bot) || (kv == m.NZ - 2 && zero_top)) {
-            val = 0.0;
-        } else {
-            const double a = class_idw(m, f, v, kv), b = class_idw(m, f, v, kv + 1);
-            val = (wB[kv] * b + wT[kv] * a) / (wT[kv] + wB[kv]);
+// out[nv + kv * nvert], kv = 0..NZ-2 (reference vertex layer kv+1).  A block
+// computes a tile of 32 vertices x 32 layers: lanes run over layers when the
+// stencil cells are read (a column's layers are contiguous, the stencil is the
+// same for the warp) and over vertices when the tile is written.
+constexpr int kVTile = 32, kVRows = 8;
+
+__global__ void __launch_bounds__(kVTile * kVRows) k_vertex_out(Mesh m, int nvert, const int* __restrict__ vcls,
+                                                               const double* __restrict__ f, int tagdir,
+                                                               const double* __restrict__ wT,
+                                                               const double* __restrict__ wB, int zero_bot,
+                                                               int zero_top, double* __restrict__ out) {
+    __shared__ double tile[kVTile][kVTile + 1];
+    const int nl = m.NZ - 1;
+    const int v0 = blockIdx.x * kVTile, kv0 = blockIdx.y * kVTile, tx = threadIdx.x;
+    for (int j = threadIdx.y; j < kVTile; j += kVRows) {
+        const int nv = v0 + j, kv = kv0 + tx;
+        if (nv < nvert && kv < nl) {
+            const int v = vcls[nv];
+            double val;
+            if (tagdir == 2) {
+                val = class_idw(m, f, v, kv);
+            } else if ((kv == 0 && zero_bot) || (kv == m.NZ - 2 && zero_top)) {
+                val = 0.0;
+            } else {
+                const double a = class_idw(m, f, v, kv), b = class_idw(m, f, v, kv + 1);
+                val = (wB[kv] * b + wT[kv] * a) / (wT[kv] + wB[kv]);
+            }
+            tile[j][tx] = val;
         }
-        out[i] = val;
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < kVTile; j += kVRows) {
+        const int nv = v0 + tx, kv = kv0 + j;
+        if (nv < nvert && kv < nl) out[(size_t)nv + (size_t)kv * nvert] = tile[tx][j];
     }
 }
 
@@ -69,7 +85,8 @@ extern "C" int nsmp_download_vertex(nsmp_ctx* c, int field, int tagdir, double* 
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(dw, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) {
-        nsmp::k_vertex_out<<<nsmp::grid_for(c, (long long)n), nsmp::kBlock, 0, c->stream>>>(
+        const dim3 tiles((NV + nsmp::kVTile - 1) / nsmp::kVTile, (NZ - 1 + nsmp::kVTile - 1) / nsmp::kVTile);
+        nsmp::k_vertex_out<<<tiles, dim3(nsmp::kVTile, nsmp::kVRows), 0, c->stream>>>(
             c->mesh, NV, c->d_vgather, c->lvl[c->ln][field - NSMP_F_U], tagdir, dw, dw + (NZ - 1), zb, zt,
             c->stage_buf);
         e = cudaGetLastError();

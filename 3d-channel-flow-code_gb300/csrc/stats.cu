@@ -13,9 +13,12 @@
 
 constexpr int kStatFields = 12;  // NSMP_S_U .. NSMP_S_EDDY
 
+constexpr int kPlaneChunks = 64;  // column chunks of the first stage of the plane sums
+
 struct StatState {
     double* sm[kStatFields] = {};
     double* plane = nullptr;
+    double* plane_part = nullptr;  // kPlaneChunks x NZ x 9 first-stage sums
     long long n = 0;
 };
 
@@ -46,31 +49,50 @@ __global__ void k_stats_sample(size_t n, StatArgs a) {
     }
 }
 
-// glob_put_plane_mm sums: one block per layer k (k0 = 1..NZ-2), the nine
-// second-order sums over the interior cells, each term divided by ns as the
-// reference does.  out[k0 * 9 + f].
+// glob_put_plane_mm sums over the interior cells of every layer k0 =
+// 1..NZ-2, the nine second-order sums divided by the sample count ns;
+// out[k0 * 9 + f].  The reference divides every term by ns; here each block
+// sum is divided once (the same value up to rounding, and 9 FP64 divisions a
+// prism less, which on this GPU's FP64 rate dominated the pass).  Two stages with a fixed order, so the
+// result is deterministic: (1) a block takes 32 consecutive layers (one per
+// lane, so a warp reads a column's layers contiguously) and one of
+// kPlaneChunks contiguous column chunks, its 8 thread rows striding over the
+// chunk's columns; the rows are summed in order into part[chunk][k0][f];
+// (2) the chunks are summed in order.
 struct PlaneArgs {
     const double* sm[9];  // u, v, w, u^2, v^2, w^2, uv, vw, wu
 };
 
-__global__ void __launch_bounds__(kBlock) k_stats_plane(Mesh m, PlaneArgs a, double ns, double* out) {
-    const int k0 = blockIdx.x + 1;
-    if (k0 > m.NZ - 2) return;
+__global__ void __launch_bounds__(256) k_stats_plane_part(Mesh m, PlaneArgs a, double ns, double* part) {
+    __shared__ double sh[8][9][33];
+    const int k0 = 1 + blockIdx.x * 32 + threadIdx.x, chunk = blockIdx.y;
+    const int c_beg = (int)((long long)m.N0 * chunk / gridDim.y);
+    const int c_end = (int)((long long)m.N0 * (chunk + 1) / gridDim.y);
     double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int c = threadIdx.x; c < m.N0; c += blockDim.x) {
-        const size_t q = IX(m, c, k0);
+    if (k0 <= m.NZ - 2)
+        for (int c = c_beg + threadIdx.y; c < c_end; c += blockDim.y) {
+            const size_t q = IX(m, c, k0);
 #pragma unroll
-        for (int f = 0; f < 9; ++f) s[f] += a.sm[f][q] / ns;
-    }
-    // block reduction, 9 values in two groups (kMaxRed-sized shared rows)
-    double g1[5] = {s[0], s[1], s[2], s[3], s[4]}, g2[4] = {s[5], s[6], s[7], s[8]};
-    block_reduce<5, false>(g1);
-    block_reduce<4, false>(g2);
-    if (threadIdx.x == 0) {
-        double* o = out + (size_t)k0 * 9;
-        for (int f = 0; f < 5; ++f) o[f] = g1[f];
-        for (int f = 0; f < 4; ++f) o[5 + f] = g2[f];
-    }
+            for (int f = 0; f < 9; ++f) s[f] += a.sm[f][q];
+        }
+#pragma unroll
+    for (int f = 0; f < 9; ++f) sh[threadIdx.y][f][threadIdx.x] = s[f] / ns;
+    __syncthreads();
+    if (threadIdx.y == 0 && k0 <= m.NZ - 2)
+        for (int f = 0; f < 9; ++f) {
+            double t = 0.0;
+            for (int y = 0; y < 8; ++y) t += sh[y][f][threadIdx.x];
+            part[((size_t)chunk * m.NZ + k0) * 9 + f] = t;
+        }
+}
+
+__global__ void k_stats_plane_sum(int nz, int nchunks, const double* __restrict__ part, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // k0 * 9 + f
+    const int k0 = i / 9;
+    if (i >= nz * 9 || k0 < 1 || k0 > nz - 2) return;
+    double t = 0.0;
+    for (int ch = 0; ch < nchunks; ++ch) t += part[(size_t)ch * nz * 9 + i];
+    out[i] = t;
 }
 
 int stats_alloc(nsmp_ctx* c) {
@@ -85,6 +107,8 @@ int stats_alloc(nsmp_ctx* c) {
     }
     CK(cudaMalloc((void**)&S.plane, (size_t)c->L.NZ * 9 * sizeof(double)));
     c->allocs.push_back(S.plane);
+    CK(cudaMalloc((void**)&S.plane_part, (size_t)kPlaneChunks * c->L.NZ * 9 * sizeof(double)));
+    c->allocs.push_back(S.plane_part);
     CK(cudaStreamSynchronize(c->stream));
     return 0;
 }
@@ -155,9 +179,12 @@ int nsmp_stats_plane(nsmp_ctx* c, double* out, double* tke) {
     nsmp::PlaneArgs a;
     const int idx[9] = {0, 1, 2, 4, 5, 6, 7, 8, 9};
     for (int f = 0; f < 9; ++f) a.sm[f] = S.sm[idx[f]];
-    nsmp::k_stats_plane<<<NZ - 2, nsmp::kBlock, 0, c->stream>>>(c->mesh, a, (double)S.n, S.plane);
+    const dim3 g1((NZ - 2 + 31) / 32, kPlaneChunks), b1(32, 8);
+    nsmp::k_stats_plane_part<<<g1, b1, 0, c->stream>>>(c->mesh, a, (double)S.n, S.plane_part);
+    nsmp::k_stats_plane_sum<<<(NZ * 9 + 255) / 256, 256, 0, c->stream>>>(NZ, kPlaneChunks, S.plane_part, S.plane);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return nsmp::cuda_fail(c, e, "k_stats_plane");
+    c->launches += 1;
     ++c->launches;
     std::vector<double> sums((size_t)NZ * 9);
     e = cudaMemcpyAsync(sums.data(), S.plane, sums.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream);

@@ -327,9 +327,14 @@ class Solver:
         self._check(self.L.nsmp_mass_diag(self.h, _p(out)))
         return out
 
-    def download_vertex(self, field, tagdir=3):
-        """Vertex values (N_VERT, NZ-1) of a level-n field (F_U .. F_P)."""
-        out = np.zeros((self.nvert, self.nz - 1), order="F")
+    def download_vertex(self, field, tagdir=3, out=None):
+        """Vertex values (N_VERT, NZ-1) of a level-n field (F_U .. F_P); into
+        `out` (float64, Fortran-ordered, e.g. pinned memory) if given."""
+        shape = (self.nvert, self.nz - 1)
+        if out is None:
+            out = np.zeros(shape, order="F")
+        elif out.dtype != np.float64 or out.shape != shape or not out.flags.f_contiguous:
+            raise ValueError("out must be a Fortran-ordered float64 array of shape %s" % (shape,))
         self._check(self.L.nsmp_download_vertex(self.h, int(field), int(tagdir), _p(out)))
         return out
 

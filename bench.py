@@ -562,6 +562,64 @@ def run_adjoint_bench(args):
     return 0
 
 
+def run_aux(args):
+    """The kernels around the path, timed on the library's stream at the
+    workload's size: turbulence-statistics sampling and plane sums, vertex
+    output (tagdir 3) with its download, and the full restart state up and
+    down.  Bytes are the compulsory ones: statistics sampling reads u, v, w,
+    p, nu_t and updates 12 FP64 sums per cell value (232 B); the plane sums
+    read 9 sums per interior prism (72 B); vertex output writes one value per
+    vertex and layer (8 B, stencil reads served by cache) and copies it to
+    pinned host memory; the state copies move the 12 arrays of the restart
+    state."""
+    import torch
+
+    import nsmp_gb300 as ng
+
+    nx, ny, layers, dt = WORKLOADS[args.workload]
+    mesh = ng.make_mesh(nx, ny)
+    prm = ng.channel_params(nx, ny, layers, dt, precision=ng.MIXED)
+    s = ng.Solver(prm, mesh)
+    u0, v0, w0, p0 = ng.initial_channel(prm, s.ncell, seed=1)
+    s.user_initial(u0, v0, w0, p0)
+    for _ in range(max(1, args.warmup)):
+        s.step(3, 1)
+    st = torch.cuda.ExternalStream(s.stream)
+    k = max(3, args.steps)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(k):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    s.stats_reset()
+    sb = StateBuffers(torch, ng, s, prm)
+    sb.download(s)
+    vbuf = torch.empty((s.nz - 1, s.nvert), dtype=torch.float64, pin_memory=True).numpy().T
+    ncv, nint, nvo = s.n0 * s.nz, s.n0 * (s.nz - 2), s.nvert * (s.nz - 1)
+    legs = {
+        "stats_sample": (s.stats_sample, 232 * ncv),
+        "stats_plane": (s.stats_plane, 72 * nint),
+        "vertex_out_tagdir3_with_download": (lambda: s.download_vertex(ng.F_U, 3, out=vbuf), 8 * nvo),
+        "upload_state": (lambda: sb.upload(s, sb.flag), sb.nbytes),
+        "download_state": (lambda: sb.download(s), sb.nbytes),
+    }
+    out = {"aux": "kernels around the path, CUDA events on the library's stream",
+           "workload": workload_desc(args.workload), "calls": k}
+    for name, (fn, nbytes) in legs.items():
+        ms = timed(fn)
+        out[name] = {"ms": round(ms, 4), "bytes": int(nbytes), "GBps": round(nbytes / (ms / 1e3) / 1e9, 1)}
+    s.close()
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -580,7 +638,11 @@ def main():
     ap.add_argument("--ckpt", type=int, default=20, help="checkpoint spacing of --adjoint-steps")
     ap.add_argument("--adjoint-budget-gb", type=float, default=0.0,
                     help="device memory for the stage inputs of an adjoint segment (0: automatic)")
+    ap.add_argument("--aux", action="store_true",
+                    help="instead of timing the step: statistics, vertex output and state copies")
     args = ap.parse_args()
+    if args.aux:
+        return run_aux(args)
     if args.accuracy_steps > 0:
         return run_accuracy(args)
     if args.adjoint_steps > 0:
