@@ -950,16 +950,19 @@ extern "C" {
 
 int nsmp_set_body_force(nsmp_ctx* c, const double* fx) {
     if (!c) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     return nsmp::run_set_body_force(c, fx);
 }
 
 int nsmp_wall_shear(nsmp_ctx* c, double* tau) {
     if (!c || !tau) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     return nsmp::run_wall_shear(c, tau);
 }
 
 int nsmp_set_adjoint_budget(nsmp_ctx* c, double bytes) {
     if (!c || bytes < 0.0) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     if (!c->adj) {
         int rc = nsmp::adj_ensure(c);
         if (rc) return rc;
@@ -970,16 +973,19 @@ int nsmp_set_adjoint_budget(nsmp_ctx* c, double bytes) {
 
 int nsmp_apply_A(nsmp_ctx* c, const double* x, double* y) {
     if (!c || !x || !y) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     return nsmp::run_apply_A(c, 0, x, y);
 }
 
 int nsmp_apply_AT(nsmp_ctx* c, const double* x, double* y) {
     if (!c || !x || !y) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     return nsmp::run_apply_A(c, 1, x, y);
 }
 
 int nsmp_adjoint(nsmp_ctx* c, int nsteps, int ckpt_every, const double* fx, double* grad_out, double* J_out) {
     if (!c || nsteps < 1 || ckpt_every < 1 || !fx) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     try {
         return nsmp::run_adjoint(c, nsteps, ckpt_every, fx, grad_out, J_out);
     } catch (...) {

@@ -36,6 +36,9 @@ int nsmp_create(const nsmp_params* prm, const nsmp_mesh* mesh, nsmp_ctx** out) {
             return NSMP_ERR_ARG;
         }
         c->precision = prm->precision;
+        // the setup makes the context's device current; the caller's
+        // current device is given back when nsmp_create returns
+        nsmp::DeviceGuard guard(c->device);
         std::string err;
         int rc = nsmp::build_layout(*prm, *mesh, c->L, err);
         if (rc != 0) {
@@ -61,6 +64,7 @@ int nsmp_create(const nsmp_params* prm, const nsmp_mesh* mesh, nsmp_ctx** out) {
 
 int nsmp_destroy(nsmp_ctx* c) {
     if (!c) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     nsmp::ctx_free(c);
     delete c;
     return NSMP_OK;
@@ -78,6 +82,7 @@ void* nsmp_stream(nsmp_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 int nsmp_host_register(nsmp_ctx* c, void* host, size_t bytes) {
     if (!c || !host || bytes == 0) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     const cudaError_t e = cudaHostRegister(host, bytes, cudaHostRegisterPortable);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -88,6 +93,7 @@ int nsmp_host_register(nsmp_ctx* c, void* host, size_t bytes) {
 
 int nsmp_host_unregister(nsmp_ctx* c, void* host) {
     if (!c || !host) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     const cudaError_t e = cudaHostUnregister(host);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -98,6 +104,7 @@ int nsmp_host_unregister(nsmp_ctx* c, void* host) {
 
 int nsmp_user_initial(nsmp_ctx* c, const double* u, const double* v, const double* w, const double* p) {
     if (!c || !u || !v || !w || !p) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     const double* in[4] = {u, v, w, p};
     for (int f = 0; f < 4; ++f) {
         int rc = nsmp::run_scatter(c, in[f], c->lvl[c->ln][f]);
@@ -113,6 +120,7 @@ int nsmp_upload_state(nsmp_ctx* c, const double* u, const double* v, const doubl
                       const double* ubf, const double* rhsu, const double* rhsv, const double* rhsw, int flag_ab) {
     if (!c || !u || !v || !w || !p || !u1f || !u2f || !u3f || !utf || !ubf || !rhsu || !rhsv || !rhsw)
         return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     // one contiguous copy and a scatter per array, one synchronisation at the
     // end (the host arrays are free for reuse when this returns)
     const double* cells[4] = {u, v, w, p};
@@ -142,6 +150,7 @@ int nsmp_upload_state(nsmp_ctx* c, const double* u, const double* v, const doubl
 
 int nsmp_download(nsmp_ctx* c, int field, double* host) {
     if (!c || !host || !valid_field(field)) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     const int NC = c->L.NC, N0 = c->L.N0;
     switch (field) {
         case NSMP_F_U: case NSMP_F_V: case NSMP_F_W: case NSMP_F_P:
@@ -168,6 +177,7 @@ int nsmp_copy_known_from_n(nsmp_ctx* c) {
 
 int nsmp_hydro_stage(nsmp_ctx* c, int* flag_ab, int fin_rk, nsmp_stage_info* info) {
     if (!c || !flag_ab || fin_rk < 1 || fin_rk > 3) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     c->flag_ab = *flag_ab;
     int rc;
     try {
@@ -187,11 +197,13 @@ int nsmp_copy_known_from_np(nsmp_ctx* c) {
 
 int nsmp_rk2_finalize(nsmp_ctx* c) {
     if (!c) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     return nsmp::run_combine(c, 0.5, 0.5);
 }
 
 int nsmp_rk_combine(nsmp_ctx* c, double a, double b) {
     if (!c) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     return nsmp::run_combine(c, a, b);
 }
 
@@ -208,6 +220,7 @@ int nsmp_time_update(nsmp_ctx* c) {
 // as the reference's RK2 does).
 int nsmp_step(nsmp_ctx* c, int fin_rk, int nsteps, int* flag_ab, nsmp_stage_info* last) {
     if (!c || fin_rk < 1 || fin_rk > 3 || nsteps < 0) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     if (flag_ab) c->flag_ab = *flag_ab;
     int worst = 0;
     for (int s = 0; s < nsteps; ++s) {
@@ -241,11 +254,13 @@ int nsmp_step(nsmp_ctx* c, int fin_rk, int nsteps, int* flag_ab, nsmp_stage_info
 
 int nsmp_mass_diag(nsmp_ctx* c, double out[4]) {
     if (!c || !out) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     return nsmp::run_mass_diag(c, out);
 }
 
 int nsmp_set_precision(nsmp_ctx* c, int mode) {
     if (!c || (mode != NSMP_FP64 && mode != NSMP_MIXED)) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     if (mode == NSMP_MIXED && !c->b64) {
         int rc = nsmp::mixed_alloc(c);
         if (rc) return rc;
@@ -265,6 +280,7 @@ int nsmp_set_inner_solver(nsmp_ctx* c, double inner_tol, int inner_cap, int rest
 
 int nsmp_prof_enable(nsmp_ctx* c, int on) {
     if (!c) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     if (c->stream) cudaStreamSynchronize(c->stream);
     nsmp::prof_resolve(c);
     c->prof_on = on ? 1 : 0;
@@ -275,6 +291,7 @@ int nsmp_prof_enable(nsmp_ctx* c, int on) {
 
 int nsmp_prof_read(nsmp_ctx* c, int kid, long long* launches, double* total_ms) {
     if (!c || kid < 0 || kid >= NSMP_K_COUNT || !launches || !total_ms) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     if (c->stream) cudaStreamSynchronize(c->stream);
     nsmp::prof_resolve(c);
     *launches = c->prof_count[kid];
@@ -301,6 +318,13 @@ int nsmp_counters(nsmp_ctx* c, long long* launches, long long* bicg_iters) {
     if (!c || !launches || !bicg_iters) return NSMP_ERR_ARG;
     *launches = c->launches;
     *bicg_iters = c->bicg_iters;
+    return NSMP_OK;
+}
+
+int nsmp_solver_counters(nsmp_ctx* c, long long* bicg_iters, long long* fp64_updates) {
+    if (!c || !bicg_iters || !fp64_updates) return NSMP_ERR_ARG;
+    *bicg_iters = c->bicg_iters;
+    *fp64_updates = c->fp64_updates;
     return NSMP_OK;
 }
 

@@ -47,7 +47,7 @@ struct nsmp_ctx {
     // hand-over: per column {kA1..3, area}, per level {dsigv, aT, aB, 0}
     float *ddcol = nullptr, *ddlev = nullptr;
     nsmp::ColPPE32* d_ppe32 = nullptr;
-    int l2_limit_set = 0;         // 1: this context raised the persisting-L2 limit (reset at destroy)
+    int l2_limit_set = 0;         // 1: this context raised the persisting-L2 limit (restored by the last such context)
     double inner_tol = 1e-1;      // FP32 residual reduction that triggers an FP64 update
     int inner_cap = 50;           // most FP32 iterations between two FP64 updates
     int restart_every = 300;      // most FP32 iterations of one Krylov process
@@ -73,6 +73,7 @@ struct nsmp_ctx {
     // launch accounting and optional per-kernel event timing
     long long launches = 0;
     long long bicg_iters = 0;
+    long long fp64_updates = 0;   // NSMP_MIXED: FP64 hand-overs (refinements) executed since creation
     int prof_on = 0;
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
@@ -93,6 +94,7 @@ int run_combine(nsmp_ctx* c, double a, double b);
 int run_gather(nsmp_ctx* c, const double* dfield, int ghost_mode, int rows, double* host);
 int run_scatter(nsmp_ctx* c, const double* host, double* dfield, int rows = 0, bool sync = true);
 int run_mass_diag(nsmp_ctx* c, double out[4]);
+int run_cfl_diag(nsmp_ctx* c, double out[NSMP_CFL_COUNT]);
 int run_mass_diag_noalloc(nsmp_ctx* c, double out[4]);
 int run_download_pv(nsmp_ctx* c, double* host);
 int cuda_fail(nsmp_ctx* c, cudaError_t e, const char* where);
@@ -109,10 +111,39 @@ int run_apply_A(nsmp_ctx* c, int transpose, const double* x, double* y);
 int run_set_body_force(nsmp_ctx* c, const double* fx);
 int run_wall_shear(nsmp_ctx* c, double* tau);
 void adj_free(nsmp_ctx* c);
+void l2_limit_release(nsmp_ctx* c);
 void stats_free(nsmp_ctx* c);
 int adj_ensure(nsmp_ctx* c);
 int prof_begin(nsmp_ctx* c, int kid);   // returns event slot or -1
 void prof_end(nsmp_ctx* c, int slot);
 int prof_resolve(nsmp_ctx* c);
 
+// Makes the context's device current for the duration of an entry point and
+// gives the caller's current device back on return, so contexts on several
+// devices can be driven from one host thread.
+struct DeviceGuard {
+    int prev = -1;
+    int dev = 0;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceGuard(int d) : dev(d) {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            prev = -1;
+            cudaGetLastError();
+        }
+        if (prev != dev) {
+            err = cudaSetDevice(dev);
+            if (err != cudaSuccess) cudaGetLastError();
+        }
+    }
+    ~DeviceGuard() {
+        if (prev >= 0 && prev != dev && cudaSetDevice(prev) != cudaSuccess) cudaGetLastError();
+    }
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
+
 }  // namespace nsmp
+
+#define NSMP_DEVICE_GUARD(ctx)                                                    \
+    nsmp::DeviceGuard nsmp_guard_((ctx)->device);                                 \
+    if (nsmp_guard_.err != cudaSuccess) return nsmp::cuda_fail((ctx), nsmp_guard_.err, "cudaSetDevice")

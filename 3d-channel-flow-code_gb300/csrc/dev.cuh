@@ -12,7 +12,7 @@ constexpr int kMaxRed = 8;    // values reduced at once
 // Per-layer factor rows of the level table (lev[row*NZ + k0]).
 enum LevRow {
     LV_DSV = 0, LV_IDSV, LV_IDST, LV_IDSB, LV_IDSBU, LV_WT, LV_WB, LV_GZP, LV_GZM, LV_HMEAN,
-    LV_DD, LV_KD, LV_DAMP, LV_IHZ, LV_ATOP, LV_ABOT, LV_COUNT
+    LV_DD, LV_KD, LV_DAMP, LV_IHZ, LV_ATOP, LV_ABOT, LV_CFLD, LV_CFLH, LV_COUNT
 };
 
 // Scalars of one stage kept in device memory between kernels.

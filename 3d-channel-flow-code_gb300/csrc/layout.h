@@ -55,7 +55,8 @@ struct ColGeo {
     double lxu[3], lyu[3];  // FVM gradient weights xnn*dlVV/area (u, w)
     double lxv[3], lyv[3];  // same for v (reference pairs faces 2/3 with dlVV 3/2)
     double area, inv_area, cbrt_area;
-    double pad;
+    int bnd;         // bit j set: edge j is a lateral boundary edge (a ghost in the reference)
+    int orig;        // original (data.txt) cell number, 0-based
 };
 
 // Per-layer factors, indexed by k0 = 1..NZ-2 (entries 0 and NZ-1 unused).
@@ -71,6 +72,8 @@ struct Levels {
     std::vector<double> les_kd;  // von_Karman*walld
     std::vector<double> les_damp;// 1-exp(-walld*Re/A+)
     std::vector<double> ihz;     // 1/dz of the FVM vertical gradient
+    std::vector<double> cfl_div; // glob_cfl lateral-flux height: dsig(k-1) as shipped (cfl.F90:139)
+    std::vector<double> cfl_h;   // glob_cfl CFL / mean / side-flux height: dsig(k) as shipped (cfl.F90:140,161)
 };
 
 struct HostLayout {

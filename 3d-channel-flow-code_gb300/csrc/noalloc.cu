@@ -1,4 +1,4 @@
-// nsmp_mass_diag_noalloc: the glob_cfl mass-flux reductions of
+// nsmp_mass_diag_noalloc: the four glob_cfl mass-flux figures of
 // nsmp_mass_diag without any allocation.
 //
 // Some callers cannot allocate device memory once their setup is done: a
@@ -8,7 +8,9 @@
 // This variant keeps its reduction scratch (per-block partial values, the
 // arrival counter and the result) in a file-scope static device array of a
 // fixed size instead of in context-allocated buffers, and calls no cudaMalloc,
-// cudaFree or allocating library routine.
+// cudaFree or allocating library routine.  Its per-prism arithmetic is the
+// shared glob_cfl restatement of diag.cuh, so its figures are those of
+// nsmp_mass_diag: the maxima bit for bit, the sums up to summation order.
 //
 // Limits and behaviour:
 //  * one thread per interior prism, 256 per block; the static array holds the
@@ -21,13 +23,16 @@
 //    contents; the arrival counter is cleared before each launch.  Calls that
 //    overlap on the GPU (several host threads, or several contexts on the
 //    same device using different streams) race on the array;
+//  * the call copies its four results to the caller's array and waits for
+//    the context's stream before it returns;
 //  * the first call on a device resolves the array's device address with
 //    cudaGetSymbolAddress (the array's name in host code is only a host-side
 //    stand-in, not a device address); make that first call before any
-//    stream capture.
+//    stream capture.  The resolved address is cached per device for the life
+//    of the process; a cudaDeviceReset by the caller would invalidate it.
 #include <mutex>
 
-#include "kern_common.cuh"
+#include "diag.cuh"
 
 namespace nsmp {
 namespace {
@@ -55,22 +60,11 @@ __global__ void __launch_bounds__(kBlock) k_mass_diag_noalloc(Mesh m, const doub
     if (g < m.nprism) {
         int c, k0;
         prism_of(m, g, c, k0);
-        const ColGeo& G = m.geo[c];
-        const size_t q = IX(m, c, k0);
-        const double dsv = lev(m, LV_DSV, k0);
-        double flux = 0.0;
-        flux = flux + f1[q] * G.L[0] * dsv;
-        flux = flux + f2[q] * G.L[1] * dsv;
-        flux = flux + f3[q] * G.L[2] * dsv;
-        flux = flux + fT[q] * G.area;
-        flux = flux + fB[q] * G.area;
-        double fc = fabs(f1[q] * G.L[0] * dsv) + fabs(f2[q] * G.L[1] * dsv) + fabs(f3[q] * G.L[2] * dsv) +
-                    fabs(fB[q] * G.area) + fabs(fT[q] * G.area);
-        fc = 0.5 * dt * fc * G.inv_area * lev(m, LV_IDSV, k0);
-        s[0] = fabs(flux);
-        s[1] = flux;
-        mx[0] = fabs(flux);
-        mx[1] = fc;
+        const CflCell o = cfl_cell(m, f1, f2, f3, fT, fB, dt, c, k0);
+        s[0] = fabs(o.flux);
+        s[1] = o.flux;
+        mx[0] = fabs(o.flux);
+        mx[1] = o.cfl;
     }
     block_reduce<2, false>(s);
     block_reduce<2, true>(mx);
@@ -125,9 +119,6 @@ int run_mass_diag_noalloc(nsmp_ctx* c, double out[4]) {
                  std::to_string((long long)kNoAllocMaxBlocks * kBlock) + " prisms";
         return NSMP_ERR_RANGE;
     }
-    int prev = 0;
-    CK(cudaGetDevice(&prev));
-    if (prev != c->device) CK(cudaSetDevice(c->device));
     double* scr = nullptr;
     int rc = scratch_addr(c, c->device, &scr);
     if (rc == 0) {
@@ -141,7 +132,6 @@ int run_mass_diag_noalloc(nsmp_ctx* c, double out[4]) {
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess) rc = cuda_fail(c, e, "nsmp_mass_diag_noalloc");
     }
-    if (prev != c->device) cudaSetDevice(prev);
     return rc;
 }
 
@@ -149,5 +139,6 @@ int run_mass_diag_noalloc(nsmp_ctx* c, double out[4]) {
 
 extern "C" int nsmp_mass_diag_noalloc(nsmp_ctx* c, double out[4]) {
     if (!c || !out) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);  // the scratch address is resolved with the context's device current
     return nsmp::run_mass_diag_noalloc(c, out);
 }

@@ -67,6 +67,7 @@ __global__ void __launch_bounds__(kVTile * kVRows) k_vertex_out(Mesh m, int nver
 
 extern "C" int nsmp_download_vertex(nsmp_ctx* c, int field, int tagdir, double* host) {
     if (!c || !host || field < NSMP_F_U || field > NSMP_F_P || (tagdir != 2 && tagdir != 3)) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     const nsmp::HostLayout& L = c->L;
     const int NZ = L.NZ, NV = L.NV;
     // blend weights of the vertex layers: dzT = |sigv(k) - sig(k+1)|, dzB = |sigv(k) - sig(k)|

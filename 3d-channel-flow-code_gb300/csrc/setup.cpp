@@ -401,7 +401,7 @@ int build_layout(const nsmp_params& p, const nsmp_mesh& m, HostLayout& L, std::s
     sigma_grid(p, L.sig.data(), L.dsig.data(), L.sigv.data(), L.dsigv.data());
     Levels& lv = L.lev;
     for (auto* a : {&lv.dsv, &lv.idsT, &lv.idsB, &lv.idsBu, &lv.wT, &lv.wB, &lv.gzp, &lv.gzm, &lv.hmean,
-                    &lv.les_dd, &lv.les_kd, &lv.les_damp, &lv.ihz})
+                    &lv.les_dd, &lv.les_kd, &lv.les_damp, &lv.ihz, &lv.cfl_div, &lv.cfl_h})
         a->assign(NZ, 0.0);
     const bool compat = p.ref_bug_compat != 0;
     const double von_karman = (double)0.415f;  // module_les.F90:33, a REAL literal
@@ -428,6 +428,11 @@ int build_layout(const nsmp_params& p, const nsmp_mesh& m, HostLayout& L, std::s
         lv.les_kd[k0] = von_karman * wd;
         lv.les_damp[k0] = 1.0 - std::exp(-(wd * 1.0 * p.re) / 26.0);
         lv.ihz[k0] = compat ? 1.0 / L.dsig[k0] : 1.0 / L.dsigv[k0 - 1];
+        // glob_cfl weights its lateral fluxes by dsig(k-1) in the divergence
+        // and by dsig(k) in the CFL number, side flux and volume means
+        // (cfl.F90:108-110, 139-140, 151, 161); the cell height is dsigv(k-1)
+        lv.cfl_div[k0] = compat ? L.dsig[k0 - 1] : L.dsigv[k0 - 1];
+        lv.cfl_h[k0] = compat ? L.dsig[k0] : L.dsigv[k0 - 1];
     }
     for (int c = 0; c < 3; ++c) {
         L.sgn_bot[c] = (p.bot_bc == 0 || c == 2) ? -1.0 : 1.0;
@@ -444,11 +449,14 @@ int build_layout(const nsmp_params& p, const nsmp_mesh& m, HostLayout& L, std::s
         const double sxx = g.sxx[i], syy = g.syy[i], sxy = g.sxy[i];
         const double det = sxx * syy - sxy * sxy;
         P.pad = 0;
+        G.bnd = 0;
+        G.orig = i;
         for (int j = 0; j < 3; ++j) {
             const int q = g.at(i, j);
             const int nbc = L.iperm[adj[i][j]];
             P.nb[j] = nbc;
             G.nb[j] = nbc;
+            if (CP(i, j) >= N0) G.bnd |= 1 << j;
             G.vtx[j] = L.vclass[g.vp[q]];
             const double co1 = g.dle1[q] / g.dlCC[q];
             P.kA[j] = co1 * g.dlVV[q];
@@ -473,7 +481,6 @@ int build_layout(const nsmp_params& p, const nsmp_mesh& m, HostLayout& L, std::s
         G.area = g.area[i];
         G.inv_area = 1.0 / g.area[i];
         G.cbrt_area = std::cbrt(g.area[i]);
-        G.pad = 0.0;
     }
 
     // reference-shaped diagnostics

@@ -37,6 +37,8 @@
 // warps and blocks in FP64.
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
 
 #include "kern_common.cuh"
 
@@ -690,13 +692,60 @@ int mixed_alloc(nsmp_ctx* c) {
     return 0;
 }
 
+// The persisting-L2 set-aside is a limit of the whole CUDA context on a
+// device, shared by every nsmp_ctx there and by the caller.  The first
+// context that raises it records the value it had; the last such context to
+// be destroyed puts that value back.
+namespace {
+struct L2Limit {
+    int users = 0;
+    size_t before = 0;
+};
+std::mutex g_l2_mu;
+std::map<int, L2Limit> g_l2;
+}  // namespace
+
+static bool l2_limit_raise(nsmp_ctx* c, size_t want) {
+    std::lock_guard<std::mutex> lk(g_l2_mu);
+    L2Limit& L = g_l2[c->device];
+    size_t cur = 0;
+    if (cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (cur >= want) return true;
+    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (!c->l2_limit_set) {
+        if (L.users == 0) L.before = cur;
+        L.users += 1;
+        c->l2_limit_set = 1;
+    }
+    return true;
+}
+
+void l2_limit_release(nsmp_ctx* c) {
+    if (!c->l2_limit_set) return;
+    std::lock_guard<std::mutex> lk(g_l2_mu);
+    L2Limit& L = g_l2[c->device];
+    c->l2_limit_set = 0;
+    if (--L.users > 0) return;
+    cudaCtxResetPersistingL2Cache();
+    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, L.before);
+    cudaGetLastError();
+}
+
 // L2 residency of D^-1 and r0 (the contiguous block of mixed_alloc) for the
 // kernels of one mixed solve, only when the whole block fits the persisting
 // set-aside the device allows.  A partial window (hit ratio below 1) on a
 // block larger than that carves persisting lines out of the L2 that the
 // neighbour gathers of both passes rely on: at 33.5M prisms (a 268 MB block)
 // it made the FP32 iteration 1.8x slower.  The destructor returns the stream
-// and the persisting lines to normal use.
+// to normal use and resets the persisting lines of the CUDA context
+// (cudaCtxResetPersistingL2Cache), which also demotes persisting lines that
+// the caller's own streams may have set.
 struct L2Window {
     nsmp_ctx* c;
     bool on = false;
@@ -710,13 +759,7 @@ struct L2Window {
         const size_t win = bytes;
         size_t lim = 0;
         if (cudaDeviceGetLimit(&lim, cudaLimitPersistingL2CacheSize) != cudaSuccess) return;
-        if (lim < std::min(win, (size_t)maxpers)) {
-            if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min(win, (size_t)maxpers)) != cudaSuccess) {
-                cudaGetLastError();
-                return;
-            }
-            c->l2_limit_set = 1;
-        }
+        if (lim < std::min(win, (size_t)maxpers) && !l2_limit_raise(c, std::min(win, (size_t)maxpers))) return;
         cudaDeviceGetLimit(&lim, cudaLimitPersistingL2CacheSize);
         cudaStreamAttrValue v{};
         v.accessPolicyWindow.base_ptr = c->invD32;

@@ -395,42 +395,14 @@ __global__ void k_gather_pv(int nvert, int nzi, const int* __restrict__ vcls, co
     }
 }
 
-// glob_cfl mass-flux check (cfl.F90:131-184) with the PPE's cell heights.
-__global__ void __launch_bounds__(kBlock) k_mass_diag(Mesh m, const double* f1, const double* f2, const double* f3,
-                                                      const double* fT, const double* fB, double dt,
-                                                      RedScratch rs, RedScratch rs2, Scal* sc) {
-    double s[2] = {0.0, 0.0}, mx[2] = {0.0, 0.0};
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
-        int c, k0;
-        prism_of(m, g, c, k0);
-        const ColGeo& G = m.geo[c];
-        const size_t q = IX(m, c, k0);
-        const double dsv = lev(m, LV_DSV, k0);
-        double flux = 0.0;
-        flux = flux + f1[q] * G.L[0] * dsv;
-        flux = flux + f2[q] * G.L[1] * dsv;
-        flux = flux + f3[q] * G.L[2] * dsv;
-        flux = flux + fT[q] * G.area;
-        flux = flux + fB[q] * G.area;
-        double fc = fabs(f1[q] * G.L[0] * dsv) + fabs(f2[q] * G.L[1] * dsv) + fabs(f3[q] * G.L[2] * dsv) +
-                    fabs(fB[q] * G.area) + fabs(fT[q] * G.area);
-        fc = 0.5 * dt * fc * G.inv_area * lev(m, LV_IDSV, k0);
-        s[0] += fabs(flux);
-        s[1] += flux;
-        mx[0] = fmax(mx[0], fabs(flux));
-        mx[1] = fmax(mx[1], fc);
-    }
-    double ts[2], tm[2];
-    if (grid_reduce<2, false>(s, rs, ts) && threadIdx.x == 0) { sc->diag[0] = ts[0]; sc->diag[2] = ts[1]; }
-    // the max reduction uses the second scratch slot: blocks may reach it
-    // while the last block of the sum is still reading its partials
-    if (grid_reduce<2, true>(mx, rs2, tm) && threadIdx.x == 0) { sc->diag[1] = tm[0]; sc->diag[3] = tm[1]; }
-}
-
 }  // namespace
 
 int cuda_fail(nsmp_ctx* c, cudaError_t e, const char* where) {
     c->err = std::string(where) + ": " + cudaGetErrorString(e);
+    // clear the runtime's last-error slot: a recoverable failure (an
+    // allocation that did not fit) must not be reported again by the next
+    // launch check of a later, correct call
+    cudaGetLastError();
     return NSMP_ERR_CUDA;
 }
 
@@ -581,6 +553,7 @@ int run_stage(nsmp_ctx* c, int fin_rk, nsmp_stage_info* info) {
     const Scal& s = *c->h_scal;
     c->last_iters = s.iter > 0 ? s.iter : 1;
     c->bicg_iters += s.iter;
+    if (c->precision == NSMP_MIXED) c->fp64_updates += s.outer;
     nsmp_stage_info inf{};
     inf.iters = s.iter;
     inf.e1norm = s.e1;
@@ -647,17 +620,6 @@ int run_scatter(nsmp_ctx* c, const double* host, double* dfield, int rows, bool 
     return 0;
 }
 
-int run_mass_diag(nsmp_ctx* c, double out[4]) {
-    const Mesh& m = c->mesh;
-    k_mass_diag<<<grid_for(c, m.nprism), kBlock, 0, c->stream>>>(m, c->face[0], c->face[1], c->face[2], c->face[3],
-                                                                c->face[4], c->prm.dt, c->red, c->red2, c->d_scal);
-    CKL("k_mass_diag");
-    CK(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(Scal), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    for (int q = 0; q < 4; ++q) out[q] = c->h_scal->diag[q];
-    return 0;
-}
-
 int ctx_init_device(nsmp_ctx* c) {
     CK(cudaSetDevice(c->device));
     CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
@@ -715,7 +677,7 @@ int ctx_init_device(nsmp_ctx* c) {
     const Levels& V = L.lev;
     const std::vector<double>* rows[LV_COUNT] = {&V.dsv, nullptr, &V.idsT, &V.idsB, &V.idsBu, &V.wT, &V.wB,
                                                  &V.gzp, &V.gzm, &V.hmean, &V.les_dd, &V.les_kd, &V.les_damp, &V.ihz,
-                                                 nullptr, nullptr};
+                                                 nullptr, nullptr, &V.cfl_div, &V.cfl_h};
     for (int r = 0; r < LV_COUNT; ++r)
         for (int k = 0; k < L.NZ; ++k) {
             double val;
@@ -757,11 +719,7 @@ void ctx_free(nsmp_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     adj_free(c);
     stats_free(c);
-    if (c->l2_limit_set) {  // the persisting-L2 set-aside is a context limit: give it back
-        cudaCtxResetPersistingL2Cache();
-        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
-        cudaGetLastError();
-    }
+    l2_limit_release(c);  // the last context that raised the persisting-L2 limit restores it
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     c->ev_pool.clear();
     for (void* p : c->allocs) cudaFree(p);

@@ -126,6 +126,7 @@ extern "C" {
 
 int nsmp_stats_reset(nsmp_ctx* c) {
     if (!c) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     int rc = nsmp::stats_alloc(c);
     if (rc) return rc;
     const size_t ncf = (size_t)c->L.N0 * c->L.NZ;
@@ -138,6 +139,7 @@ int nsmp_stats_reset(nsmp_ctx* c) {
 
 int nsmp_stats_sample(nsmp_ctx* c) {
     if (!c) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     int rc = nsmp::stats_alloc(c);
     if (rc) return rc;
     nsmp::StatArgs a;
@@ -161,6 +163,7 @@ int nsmp_stats_count(nsmp_ctx* c, int* n) {
 
 int nsmp_stats_download(nsmp_ctx* c, int which, double* host) {
     if (!c || !host || which < 0 || which >= kStatFields) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     int rc = nsmp::stats_alloc(c);
     if (rc) return rc;
     return nsmp::run_gather(c, c->stats->sm[which], 1, c->L.NC, host);
@@ -168,6 +171,7 @@ int nsmp_stats_download(nsmp_ctx* c, int which, double* host) {
 
 int nsmp_stats_plane(nsmp_ctx* c, double* out, double* tke) {
     if (!c || !out) return NSMP_ERR_ARG;
+    NSMP_DEVICE_GUARD(c);
     int rc = nsmp::stats_alloc(c);
     if (rc) return rc;
     StatState& S = *c->stats;

@@ -65,8 +65,13 @@ EXPORTS = [
     "nsmp_set_inner_solver", "nsmp_solver_log", "nsmp_mass_diag_noalloc",
     "nsmp_set_body_force", "nsmp_wall_shear", "nsmp_adjoint", "nsmp_apply_A", "nsmp_apply_AT",
     "nsmp_set_adjoint_budget", "nsmp_stats_reset", "nsmp_stats_sample", "nsmp_stats_count",
-    "nsmp_stats_download", "nsmp_stats_plane", "nsmp_download_vertex",
+    "nsmp_stats_download", "nsmp_stats_plane", "nsmp_download_vertex", "nsmp_cfl_diag",
+    "nsmp_solver_counters", "nsmp_probe_fp64_fma",
 ]
+
+# glob_cfl values of nsmp_cfl_diag (NSMP_CFL_* order)
+CFL_NAMES = ["umax", "vmax", "wmax", "aveu", "avev", "avew", "cfl_max", "flux_total", "flux_max", "flux_bc",
+             "flux_bot", "flux_top", "flux_side", "abs_div"]
 
 (K_VERTEX4, K_STAGE_RHS, K_FACES_DIV, K_BICG_INIT, K_BICG_P, K_BICG_SPMV_V, K_BICG_S, K_BICG_SPMV_T,
  K_BICG_X, K_PMEAN, K_VERTEX1, K_PROJECT, K_IN_PV, K_IN_ST, K_MIX_UPDATE, K_MIX_SCALE, K_OTHER,
@@ -111,6 +116,7 @@ def lib(build_if_missing=True):
     L.nsmp_step.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(StageInfo)]
     L.nsmp_mass_diag.argtypes = [vp, vp]
     L.nsmp_mass_diag_noalloc.argtypes = [vp, vp]
+    L.nsmp_cfl_diag.argtypes = [vp, vp]
     L.nsmp_set_precision.argtypes = [vp, C.c_int]
     L.nsmp_set_inner_solver.argtypes = [vp, C.c_double, C.c_int, C.c_int]
     L.nsmp_set_body_force.argtypes = [vp, vp]
@@ -139,6 +145,8 @@ def lib(build_if_missing=True):
     L.nsmp_prof_read.argtypes = [vp, C.c_int, P(C.c_longlong), P(C.c_double)]
     L.nsmp_counters.argtypes = [vp, P(C.c_longlong), P(C.c_longlong)]
     L.nsmp_solver_log.argtypes = [vp, C.c_int, vp, vp, vp, vp]
+    L.nsmp_solver_counters.argtypes = [vp, P(C.c_longlong), P(C.c_longlong)]
+    L.nsmp_probe_fp64_fma.argtypes = [C.c_int, C.c_int, P(C.c_double), P(C.c_double)]
     _lib = L
     return L
 
@@ -215,6 +223,15 @@ def initial_channel(params, n_cell, umax=18.0, amp=1.8, seed=1):
     if rc:
         raise RuntimeError(f"nsmp_initial_channel failed ({rc})")
     return arrs
+
+
+def probe_fp64_fma(device=0, iters=20000):
+    """Measured FP64 FMA rate of a device in TFLOP/s (nsmp_probe_fp64_fma)."""
+    t, ms = C.c_double(), C.c_double()
+    rc = lib().nsmp_probe_fp64_fma(device, iters, C.byref(t), C.byref(ms))
+    if rc:
+        raise RuntimeError(f"nsmp_probe_fp64_fma failed ({rc})")
+    return t.value, ms.value
 
 
 class NsmpError(RuntimeError):
@@ -323,9 +340,16 @@ class Solver:
         return rc, info.as_dict()
 
     def mass_diag(self):
+        """(sum |div|, max |div|, sum div, max CFL) of glob_cfl."""
         out = np.zeros(4, dtype=np.float64)
         self._check(self.L.nsmp_mass_diag(self.h, _p(out)))
         return out
+
+    def cfl_diag(self):
+        """glob_cfl (cfl.F90) on the level-n state: dict of the CFL_NAMES values."""
+        out = np.zeros(len(CFL_NAMES), dtype=np.float64)
+        self._check(self.L.nsmp_cfl_diag(self.h, _p(out)))
+        return dict(zip(CFL_NAMES, out.tolist()))
 
     def download_vertex(self, field, tagdir=3, out=None):
         """Vertex values (N_VERT, NZ-1) of a level-n field (F_U .. F_P); into
@@ -439,6 +463,12 @@ class Solver:
         ac = np.zeros(n, np.int32)
         k = self._check(self.L.nsmp_solver_log(self.h, n, _p(it), _p(ri), _p(ro), _p(ac)))
         return list(zip(it[:k].tolist(), ri[:k].tolist(), ro[:k].tolist(), ac[:k].tolist()))
+
+    def solver_counters(self):
+        """(BiCGSTAB iterations, FP64 hand-overs of the mixed solver) since creation."""
+        a, b = C.c_longlong(), C.c_longlong()
+        self._check(self.L.nsmp_solver_counters(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def counters(self):
         """(kernel launches, BiCGSTAB iterations) since creation."""

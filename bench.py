@@ -156,54 +156,88 @@ def workload_desc(name):
             f"BiCGSTAB-Jacobi eps=1e-10")
 
 
-def cpu_oracle_sample(name, nthreads, max_seconds=30.0):
-    """Time the CPU oracle on the same workload: the first stage (Euler
-    predictor + full PPE solve) of step 1.  Returns seconds per stage."""
-    import nsmp_gb300 as ng
+def cpu_model():
+    """One-line description of the host CPU (model name or Arm part)."""
+    try:
+        txt = open("/proc/cpuinfo").read()
+    except OSError:
+        return "unknown"
+    for key in ("model name", "Model", "CPU part"):
+        for ln in txt.splitlines():
+            if ln.lower().startswith(key.lower()):
+                val = ln.split(":", 1)[1].strip()
+                return f"{key}: {val}" if key == "CPU part" else val
+    return "unknown"
+
+
+def oracle_workload(name, nthreads):
+    """The CPU oracle on the workload, built from the oracle's own synthetic
+    inputs (bit-identical to the library's), so no product code is loaded."""
     from oracle import oracle_ctypes as oc
     nx, ny, layers, dt = WORKLOADS[name]
-    mesh = ng.make_mesh(nx, ny)
-    prm = ng.channel_params(nx, ny, layers, dt)
-    okeys = [k for k, _ in oc.OrcParams._fields_ if k != "nthreads"]
-    o = oc.Oracle({k: prm[k] for k in okeys}, mesh, nthreads=nthreads)
-    u, v, w, p = ng.initial_channel(prm, o.ncell, seed=1)
-    o.user_initial(u, v, w, p)
-    t0 = time.perf_counter()
-    _, info = o.step(1)
-    t = time.perf_counter() - t0
-    return t, info
+    o = oc.Oracle(oc.channel_params(nx, ny, layers, dt), oc.make_mesh(nx, ny), nthreads=nthreads)
+    return o, oc
 
 
 def run_reference(args):
-    """CPU arm: the reference's algorithm on the host cores (the oracle port,
-    since no Fortran toolchain exists to build the reference itself)."""
+    """CPU arm: the reference's algorithm on the host cores -- the oracle
+    port, since no Fortran toolchain exists to build the reference itself.
+    From the same seeded initial state as the GPU arm it runs W full RK3
+    warm-up steps, then times K full RK3 steps (all three stages with their
+    PPE solves): the same steps the GPU arm times."""
     world, rank, local, pg = dist_setup()
     if rank != 0:
         return 0
-    nthreads = os.cpu_count() or 1
+    nthreads = args.ref_threads or os.cpu_count() or 1
     nx, ny, layers, dt = WORKLOADS[args.workload]
     prisms = 2 * nx * ny * layers
+    o, oc = oracle_workload(args.workload, nthreads)
+    o.user_initial(*o.initial_channel(seed=1))
+    warm = []
     for _ in range(args.warmup):
-        cpu_oracle_sample(args.workload, nthreads)
-    times, iters = [], []
+        rc, info = o.step(3)
+        warm.append(info["iters_stage"])
+    stages = []
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        t, info = cpu_oracle_sample(args.workload, nthreads)
-        times.append(t)
-        iters.append(info["iters"])
-    t_stage = float(np.median(times))
-    value = prisms / (3.0 * t_stage) / 1e6
+        rc, info = o.step(3)
+        stages.append(info["iters_stage"])
+    t = time.perf_counter() - t0
+    value = prisms * args.steps / t / 1e6
+    its = float(np.mean(stages)) if stages else 0.0
     line = {
         "impl": "reference", "metric": "Mcell-steps/s", "value": value, "unit": "Mcell-steps/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 3.0 * t_stage * 1e3,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / max(args.steps, 1) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_desc(args.workload), "prisms": prisms},
+        "config": {"workload": workload_desc(args.workload), "prisms": prisms,
+                   "integrator": "SSP-RK3 of the reference stage", "bicgstab_iters_per_stage": round(its, 1)},
+        "bicgstab_iters_per_stage_timed": stages, "bicgstab_iters_per_stage_warmup": warm,
         "cpu_baseline": {"value": value, "unit": "Mcell-steps/s", "cores": nthreads, "kind": "port",
-                         "sample": "per step: stage 1 of step 1 (predictor + PPE solve to 1e-10, "
-                                   f"{int(np.median(iters))} BiCGSTAB iterations) x3 stages/step"},
+                         "cpu": cpu_model(),
+                         "sample": f"{args.steps} full RK3 steps (3 stages, PPE to 1e-10) after {args.warmup} "
+                                   f"warm-up steps from the seeded initial state, wall clock"},
         "e2e": {"value": value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def cpu_step_from_state(args, snap, nthreads):
+    """The oracle on one full RK3 step from the state the GPU arm's timed
+    region started from (uploaded into the oracle): the same work as the
+    first timed GPU step.  Returns (seconds, per-stage iterations)."""
+    o, oc = oracle_workload(args.workload, nthreads)
+    for a, f in zip(snap.cells, (oc.F_U, oc.F_V, oc.F_W, oc.F_P)):
+        o.set(f, a)
+    for a, f in zip(snap.faces, (oc.F_U1F, oc.F_U2F, oc.F_U3F, oc.F_UTF, oc.F_UBF)):
+        o.set(f, a)
+    for a, f in zip(snap.hist, (oc.F_RHSU, oc.F_RHSV, oc.F_RHSW)):
+        o.set(f, a)
+    o.set(oc.F_PV, snap.pv)
+    o.flag_ab = snap.flag
+    t0 = time.perf_counter()
+    rc, info = o.step(3)
+    return time.perf_counter() - t0, info["iters_stage"]
 
 
 # Mixed solver, in 8-byte words per prism.  k_in_pv: s, t, p, v, D^-1 (stencil),
@@ -245,6 +279,11 @@ class StateBuffers:
                 s.download(f, out=a)
         self.flag = s.flag_ab
 
+    def keep_vertex_pressure(self, s, ng):
+        """The vertex pressure of the last stage (the lagged pf of
+        update_rhsp), for a CPU run that continues from this state."""
+        self.pv = s.download(ng.F_PV)
+
     def upload(self, s, flag):
         s.upload_state(*self.cells, self.faces, self.hist, flag)
 
@@ -257,6 +296,7 @@ def timed_region(s, ng, torch, stream, steps, pg, local, profile=False):
     region run without them."""
     s.prof_enable(profile)
     l0, it0 = s.counters()
+    _, up0 = s.solver_counters()
     clocks = ClockSampler(local)
     clocks.start()
     torch.cuda.synchronize()
@@ -276,12 +316,41 @@ def timed_region(s, ng, torch, stream, steps, pg, local, profile=False):
     ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
     l1, it1 = s.counters()
+    _, up1 = s.solver_counters()
     prof = s.prof_read() if profile else None
     s.prof_enable(False)
-    return {"ms": ms, "clocks": clk, "launches": l1 - l0, "iters": it1 - it0, "prof": prof, "status": worst}
+    return {"ms": ms, "clocks": clk, "launches": l1 - l0, "iters": it1 - it0, "updates": up1 - up0, "prof": prof,
+            "status": worst}
 
 
-def roofline(prof, iters, prisms, mixed):
+# Kernels that run once per BiCGSTAB iteration (their launches after the
+# device-side stopping test return at once and move nothing), and the mixed
+# solver's FP64 hand-over kernels, which act once per refinement update.
+ITER_KERNELS = ("k_bicg_p", "k_bicg_spmv_v", "k_bicg_s", "k_bicg_spmv_t", "k_bicg_x", "k_in_pv", "k_in_st")
+UPDATE_KERNELS = ("k_mix_update", "k_mix_scale")
+
+
+def step_bytes(prof, iters, updates, steps, prisms, mixed):
+    """Algorithmic bytes of the K steps of a region: every kernel's words per
+    prism (WORDS, WORDS_MIXED) x 8 B x prisms x the times it did work --
+    iterations for the iteration passes, FP64 updates for the hand-over
+    kernels, launches for the rest (the kernels around the solve run once
+    per stage; 'other' holds the RK combinations, 3 words per cell each).
+    Returns (bytes per step, bytes per iteration, bytes per update, fixed
+    bytes per step)."""
+    words = dict(WORDS)
+    if mixed:
+        words.update(WORDS_MIXED)
+        words["k_bicg_init"] = 2 + 2  # k_mix_init: rhsp, pf read; b, x written
+    words["other"] = 3
+    per_iter = sum(words[k] for k in ITER_KERNELS if k in words and prof.get(k, (0, 0))[0] > 0) * 8.0 * prisms
+    per_upd = sum(words[k] for k in UPDATE_KERNELS if prof.get(k, (0, 0))[0] > 0) * 8.0 * prisms
+    fixed = sum(words[k] * 8.0 * prisms * prof[k][0] for k in prof
+                if k in words and k not in ITER_KERNELS and k not in UPDATE_KERNELS) / max(steps, 1)
+    return fixed + (per_iter * iters + per_upd * updates) / max(steps, 1), per_iter, per_upd, fixed
+
+
+def roofline(prof, iters, prisms, mixed, fp64_peak=None):
     hbm_peak, peak_kind = load_peaks()
     words = dict(WORDS)
     if mixed:
@@ -308,6 +377,12 @@ def roofline(prof, iters, prisms, mixed):
             "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind, "traffic": traffic,
             "algorithmic_bytes_per_launch": bpl, "avg_launch_ms": dom_ms / max(real, 1),
             "fp64_tflops": (round(fl * prisms * real / (dom_ms / 1e3) / 1e12, 3) if fl and dom_ms > 0 else None)}
+    if roof["fp64_tflops"] is not None and fp64_peak:
+        # the FP64 passes are bound by min(HBM, FP64 issue): both fractions
+        roof["fp64_peak_tflops"] = round(fp64_peak, 3)
+        roof["fp64_peak_kind"] = "measured in this run (nsmp_probe_fp64_fma, FMA chains, CUDA events)"
+        roof["fp64_frac"] = round(roof["fp64_tflops"] / fp64_peak, 4)
+        roof["bound"] = "fp64" if roof["fp64_frac"] > roof["frac"] else "hbm"
     return roof, shares, total
 
 
@@ -325,6 +400,7 @@ def run_ours(args):
     head = "mixed" if "mixed" in precs else precs[0]
     res, solvers = {}, {}
     snap = u_end = None
+    fp64_peak, _ = ng.probe_fp64_fma(local)
     for prec in precs:
         prm = ng.channel_params(nx, ny, layers, dt, device=local,
                                 precision=(ng.MIXED if prec == "mixed" else ng.FP64))
@@ -339,6 +415,7 @@ def run_ours(args):
         if prec == head:  # the state the timed steps start from, for the end-to-end replay
             snap = StateBuffers(torch, ng, s, prm)
             snap.download(s)
+            snap.keep_vertex_pressure(s, ng)
         r = timed_region(s, ng, torch, stream, args.steps, pg, local)
         if prec == head:
             u_end = s.download(ng.F_U)
@@ -347,7 +424,17 @@ def run_ours(args):
         # per-kernel device times over K further steps of the same run
         rp = timed_region(s, ng, torch, stream, args.steps, pg, local, profile=True)
         r["prof"], r["prof_ms"], r["prof_iters"] = rp["prof"], rp["ms"], rp["iters"]
-        r["roof"], r["shares"], r["busy_ms"] = roofline(rp["prof"], rp["iters"], prisms, prec == "mixed")
+        r["roof"], r["shares"], r["busy_ms"] = roofline(rp["prof"], rp["iters"], prisms, prec == "mixed",
+                                                        fp64_peak)
+        # whole step: the timed region's iterations and FP64 updates with the
+        # per-kernel bytes of the profiled region
+        _, b_it, b_up, b_fix = step_bytes(rp["prof"], rp["iters"], rp["updates"], args.steps, prisms,
+                                          prec == "mixed")
+        bstep = b_fix + (b_it * r["iters"] + b_up * r["updates"]) / args.steps
+        hbm_peak, _ = load_peaks()
+        r["roof"]["step_bytes"] = bstep
+        r["roof"]["step_achieved"] = round(bstep / (r["ms_max"] / args.steps / 1e3) / 1e9, 1)
+        r["roof"]["step_frac"] = round(bstep / (r["ms_max"] / args.steps / 1e3) / 1e9 / hbm_peak, 4)
         res[prec] = r
         solvers[prec] = (s, stream, prm)
     s, stream, prm = solvers[head]
@@ -403,11 +490,11 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         nthreads = os.cpu_count() or 1
-        t_stage, cinfo = cpu_oracle_sample(args.workload, nthreads)
-        cpu = {"value": prisms / (3.0 * t_stage) / 1e6, "unit": "Mcell-steps/s", "cores": nthreads,
-               "kind": "port",
-               "sample": f"stage 1 of step 1 of the same workload ({cinfo['iters']} BiCGSTAB iterations, "
-                         f"{t_stage:.1f} s), scaled x3 stages per step"}
+        t_cpu, cits = cpu_step_from_state(args, snap, nthreads)
+        cpu = {"value": prisms / t_cpu / 1e6, "unit": "Mcell-steps/s", "cores": nthreads, "kind": "port",
+               "cpu": cpu_model(), "bicgstab_iters_per_stage": cits,
+               "sample": f"one full RK3 step ({t_cpu:.1f} s wall clock) of the oracle from the state the timed "
+                         f"region started from: the first timed step's work"}
 
     if rank == 0:
         line = {
@@ -457,6 +544,8 @@ def run_accuracy(args):
     nx, ny, layers, dt = WORKLOADS[args.workload]
     mesh = ng.make_mesh(nx, ny)
     sol = {}
+    clocks = ClockSampler(0)
+    clocks.start()
     for prec in ("fp64", "mixed"):
         prm = ng.channel_params(nx, ny, layers, dt, precision=(ng.MIXED if prec == "mixed" else ng.FP64))
         s = ng.Solver(prm, mesh)
@@ -469,7 +558,7 @@ def run_accuracy(args):
             worst = max(worst, rc)
         sol[prec] = {"fields": {nm: s.download(f)[:prm["n0"], 1:-1] for nm, f in
                                 (("u", ng.F_U), ("v", ng.F_V), ("w", ng.F_W), ("p", ng.F_P))},
-                     "div": s.mass_diag(), "status": worst, "s": time.perf_counter() - t0}
+                     "div": s.mass_diag(), "cfl": s.cfl_diag(), "status": worst, "s": time.perf_counter() - t0}
         s.close()
     a, b = sol["mixed"], sol["fp64"]
     out = {"accuracy": "mixed vs fp64", "workload": workload_desc(args.workload), "steps": args.accuracy_steps}
@@ -479,6 +568,8 @@ def run_accuracy(args):
     out["max_div_diff"] = abs(out["max_div_mixed"] - out["max_div_fp64"])
     out["status"] = {"mixed": a["status"], "fp64": b["status"]}
     out["wall_s"] = {"mixed": round(a["s"], 1), "fp64": round(b["s"], 1)}
+    out["clocks"] = clocks.stop()
+    out["cfl_mixed"], out["cfl_fp64"] = a["cfl"], b["cfl"]
     print(json.dumps(out), flush=True)
     return 0
 
@@ -523,7 +614,10 @@ def run_adjoint_bench(args):
     s.step(3, 1)  # warm-up (first-use allocations, occupancy queries)
     s.upload_state(*cells, faces, hist, 0)
     l0, i0 = s.counters()
+    clocks = ClockSampler(0)
+    clocks.start()
     t_fwd, _ = timed(lambda: [s.step(3, 1) for _ in range(N)])
+    clk_fwd = clocks.stop()
     l1, i1 = s.counters()
     s.upload_state(*cells, faces, hist, 0)
     # device memory in use while the adjoint runs (sampled every 50 ms)
@@ -538,9 +632,12 @@ def run_adjoint_bench(args):
 
     th = threading.Thread(target=poll, daemon=True)
     th.start()
+    clocks = ClockSampler(0)
+    clocks.start()
     t_adj, (J, grad, rc) = timed(lambda: s.adjoint(N, K, fx))
     stop.set()
     th.join()
+    clk_adj = clocks.stop()
     l2, i2 = s.counters()
     ncf = n0 * nz
     nseg = -(-N // K)
@@ -556,7 +653,8 @@ def run_adjoint_bench(args):
             "peak_device_bytes_in_use": total - free_min[0],
             "segment_budget_bytes": args.adjoint_budget_gb * 1e9 or "80% of free memory",
             "gpu_launches": l2 - l1, "dtype": "f32+f64" if mixed else "f64",
-            "precision": "mixed forward and adjoint solves, FP64 adjoint accumulation" if mixed else "fp64"}
+            "precision": "mixed forward and adjoint solves, FP64 adjoint accumulation" if mixed else "fp64",
+            "clocks": {"forward": clk_fwd, "adjoint": clk_adj}}
     print(json.dumps(line), flush=True)
     s.close()
     return 0
@@ -571,7 +669,7 @@ def run_aux(args):
     read 9 sums per interior prism (72 B); vertex output writes one value per
     vertex and layer (8 B, stencil reads served by cache) and copies it to
     pinned host memory; the state copies move the 12 arrays of the restart
-    state."""
+    state; glob_cfl reads the five face fluxes and u, v, w (64 B a prism)."""
     import torch
 
     import nsmp_gb300 as ng
@@ -609,14 +707,33 @@ def run_aux(args):
         "vertex_out_tagdir3_with_download": (lambda: s.download_vertex(ng.F_U, 3, out=vbuf), 8 * nvo),
         "upload_state": (lambda: sb.upload(s, sb.flag), sb.nbytes),
         "download_state": (lambda: sb.download(s), sb.nbytes),
+        "cfl_diag": (s.cfl_diag, 8 * 8 * nint),
     }
     out = {"aux": "kernels around the path, CUDA events on the library's stream",
            "workload": workload_desc(args.workload), "calls": k}
+    clocks = ClockSampler(0)
+    clocks.start()
     for name, (fn, nbytes) in legs.items():
         ms = timed(fn)
         out[name] = {"ms": round(ms, 4), "bytes": int(nbytes), "GBps": round(nbytes / (ms / 1e3) / 1e9, 1)}
+    out["clocks"] = clocks.stop()
     s.close()
     print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_fp64_peak(args):
+    """FP64 FMA issue rate of the device (the roof of the FP64 solver passes),
+    measured over several repetitions with clocks sampled."""
+    import nsmp_gb300 as ng
+    clocks = ClockSampler(0)
+    clocks.start()
+    runs = [ng.probe_fp64_fma(0, 200000) for _ in range(max(3, args.steps))]
+    clk = clocks.stop()
+    best = max(t for t, _ in runs)
+    print(json.dumps({"fp64_fma_peak": "FP64 FMA chains, full-device grid, CUDA events", "tflops_best": best,
+                      "tflops_median": float(np.median([t for t, _ in runs])),
+                      "ms_per_run": [round(m, 3) for _, m in runs], "clocks": clk}), flush=True)
     return 0
 
 
@@ -628,6 +745,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--ref-threads", type=int, default=0,
+                    help="host threads of the --impl reference arm (0: all cores)")
+    ap.add_argument("--fp64-peak", action="store_true",
+                    help="instead of timing the step: the device's FP64 FMA rate with clocks sampled")
     ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"])
     ap.add_argument("--profile-run", action="store_true",
                     help="device-timed region only (no end-to-end leg, no CPU baseline), for ncu captures")
@@ -641,6 +762,8 @@ def main():
     ap.add_argument("--aux", action="store_true",
                     help="instead of timing the step: statistics, vertex output and state copies")
     args = ap.parse_args()
+    if args.fp64_peak:
+        return run_fp64_peak(args)
     if args.aux:
         return run_aux(args)
     if args.accuracy_steps > 0:

@@ -145,12 +145,38 @@ int nsmp_time_update(nsmp_ctx* ctx);         /* LoopTimeUpdate.F90:228-250 */
  * (the switch of hydro.F90:469-478); NULL keeps the context's flag. */
 int nsmp_step(nsmp_ctx* ctx, int fin_rk, int nsteps, int* flag_ab, nsmp_stage_info* last);
 
-/* glob_cfl mass-flux reductions (cfl.F90:131-184), FP64 on the device:
- * out[0] = sum|div|, out[1] = max|div|, out[2] = sum div, out[3] = max CFL. */
+/* Indices of the values nsmp_cfl_diag returns. */
+enum {
+    NSMP_CFL_UMAX = 0,      /* signed u of largest |u| (first in loop order)    cfl.F90:99     */
+    NSMP_CFL_VMAX,          /* signed v of largest |v|                          cfl.F90:100    */
+    NSMP_CFL_WMAX,          /* signed w of largest |w|                          cfl.F90:101    */
+    NSMP_CFL_AVEU,          /* sum u area h / (TotalVolume (SigFin-SigIni)), the meanuv.dat columns */
+    NSMP_CFL_AVEV,          /*                                                  cfl.F90:108-110, 186-189 */
+    NSMP_CFL_AVEW,
+    NSMP_CFL_MAX,           /* max CFL, 0.5 dt sum|face flux| / (area h)        cfl.F90:140-166 */
+    NSMP_CFL_FLUX_TOTAL,    /* "Total flux": sum of the cells' net outflow      cfl.F90:138-165 */
+    NSMP_CFL_FLUX_MAX,      /* "Maxim flux": signed net outflow of largest modulus  cfl.F90:167-168 */
+    NSMP_CFL_FLUX_BC,       /* "BC flux" = BOT + TOP + Side                     cfl.F90:215    */
+    NSMP_CFL_FLUX_BOT,      /* sum UBFACE area at k = 2                         cfl.F90:171-175 */
+    NSMP_CFL_FLUX_TOP,      /* sum UTFACE area at k = NZ-1                      cfl.F90:177-181 */
+    NSMP_CFL_FLUX_SIDE,     /* face flux through the lateral boundary edges     cfl.F90:141-150 */
+    NSMP_CFL_ABS_DIV,       /* sum of |net outflow| (not printed by glob_cfl)   */
+    NSMP_CFL_COUNT
+};
+/* glob_cfl (Main/cfl.F90:7-269) on the level-n velocities and the face
+ * fluxes, FP64 on the device, out[NSMP_CFL_COUNT].  With ref_bug_compat the
+ * lateral fluxes of the divergence are weighted by dsig(k-1) and everything
+ * else by dsig(k), as shipped (cfl.F90:108-110, 139-140); without it both use
+ * the cell height dsigv(k-1).  Maxima equal the reference's exactly; sums
+ * differ from its running accumulators by summation order only. */
+int nsmp_cfl_diag(nsmp_ctx* ctx, double* out);
+/* The four mass-flux figures of nsmp_cfl_diag: out[0] = sum|div|,
+ * out[1] = max|div| (= |Maxim flux|), out[2] = sum div (Total flux),
+ * out[3] = max CFL. */
 int nsmp_mass_diag(nsmp_ctx* ctx, double out[4]);
 int nsmp_set_precision(nsmp_ctx* ctx, int mode);
-/* The reductions of nsmp_mass_diag without any allocation (no counterpart in
- * the reference).  For callers that cannot allocate device memory after
+/* The four figures of nsmp_mass_diag without any allocation (no counterpart
+ * in the reference).  For callers that cannot allocate device memory after
  * setup -- a driver that reserves a fixed device-memory budget before its
  * time loop, or one that forbids allocation inside the loop because it can
  * synchronise the device -- the reduction scratch lives in a static device
@@ -158,8 +184,9 @@ int nsmp_set_precision(nsmp_ctx* ctx, int mode);
  * most 16,777,216 prisms (65536 blocks of 256); larger ones get
  * NSMP_ERR_RANGE.  The array (about 2 MB) stays on every GPU that loaded the
  * library until exit.  All calls share it, so calls that overlap on the GPU
- * race; the first call on a device resolves the array's address and should
- * come before any stream capture. */
+ * race.  The call copies its four results to `out` and waits for the
+ * context's stream before returning.  The first call on a device resolves
+ * the array's address and should come before any stream capture. */
 int nsmp_mass_diag_noalloc(nsmp_ctx* ctx, double out[4]);
 /* NSMP_MIXED pressure solver.  The FP32 BiCGSTAB hands its correction e to
  * FP64 when its residual fell by inner_tol since the last hand-over (default
@@ -267,6 +294,15 @@ int nsmp_solver_log(nsmp_ctx* ctx, int max_cycles, int* inner_iters, double* inn
                     double* outer_res, int* accepted);
 /* Kernels launched and BiCGSTAB iterations executed since creation. */
 int nsmp_counters(nsmp_ctx* ctx, long long* launches, long long* bicg_iters);
+/* BiCGSTAB iterations and, in NSMP_MIXED, FP64 hand-overs (refinement
+ * updates) executed since creation. */
+int nsmp_solver_counters(nsmp_ctx* ctx, long long* bicg_iters, long long* fp64_updates);
+/* Measured FP64 FMA issue rate of a device: every thread of a full-device
+ * grid runs `chains` independent chains of `iters` dependent fused
+ * multiply-adds, timed with CUDA events; *tflops = 2 x FMAs / time.  No
+ * context needed.  The roof for the FP64 kernels that are bound by FP64
+ * issue rather than by HBM. */
+int nsmp_probe_fp64_fma(int device, int iters, double* tflops, double* ms);
 
 /* ---- synthetic inputs (host only, no GPU needed) ------------------------ */
 

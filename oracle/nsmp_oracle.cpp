@@ -8,8 +8,13 @@
 //
 // Parity with the reference binary is UNPINNED: the reference ships no tests,
 // golden vectors or input decks, and no Fortran toolchain exists here.  Pins
-// available: Functions.F90 analytic fields and the reference's own asserted
-// invariants (see tests/test_oracle.py).
+// available: the Functions.F90 analytic fields and the reference's own asserted
+// invariants (tests/test_oracle_known_answers.py, tests/test_setup_geometry.py).
+//
+// The same file carries the oracle's own copy of the synthetic inputs (the
+// jittered periodic mesh and the seeded channel state), so the CPU baseline
+// runs without loading the product library; tests check that both copies
+// produce the same bits.
 //
 // Deliberate deviations (all below 1e-15 relative per operation):
 //  * global sums are formed as per-layer partial sums added in layer order
@@ -1143,16 +1148,17 @@ void newu3D(orc_ctx& c, R2& fun, R2& funv, const R2& dpdx, const R2& dpdy) {
         }
 }
 
-// hydro: Main/hydro.F90:197-478 (one stage).
-void hydro(orc_ctx& c, int fin_rk) {
+// Predictor part of hydro (Main/hydro.F90:225-342): eddy viscosity,
+// advection-diffusion right-hand side and the Euler/AB2 predictor
+// u* = u + dt (c1 rhs + c2 rhs_old); updates the AB2 history.
+void predictor(orc_ctx& c, R2& ufstar, R2& vfstar, R2& wfstar) {
     const int N0 = c.N0, NZ = c.NZ, NC = c.NC;
     const orc_params& P = c.P;
     double c1, c2;
     if (c.flag_ab == 1) { c1 = 1.55; c2 = -0.55; }
     else { c1 = 1.0; c2 = 0.0; }
-    R2 ufstar, vfstar, wfstar, Gam, rhsu, rhsv, rhsw, rhsp, dpdx, dpdy, dpds;
-    for (R2* a : {&ufstar, &vfstar, &wfstar, &Gam, &rhsu, &rhsv, &rhsw, &rhsp, &dpdx, &dpdy, &dpds})
-        a->init(NC, NZ);
+    R2 Gam, rhsu, rhsv, rhsw;
+    for (R2* a : {&Gam, &rhsu, &rhsv, &rhsw}) a->init(NC, NZ);
     c.info.max_eddy = 0.0;
     if (P.les) sgles(c, c.uf, c.vf, c.wf);
     const double invRe = 1.0 / P.re;
@@ -1178,6 +1184,15 @@ void hydro(orc_ctx& c, int fin_rk) {
             wfstar(i, k) = wfstar(i, k) + P.dt * (c1 * rhsw(i, k) + c2 * c.rhswf(i, k));
             c.rhswf(i, k) = rhsw(i, k);
         }
+}
+
+// hydro: Main/hydro.F90:197-478 (one stage).
+void hydro(orc_ctx& c, int fin_rk) {
+    const int N0 = c.N0, NZ = c.NZ, NC = c.NC;
+    const orc_params& P = c.P;
+    R2 ufstar, vfstar, wfstar, rhsp, dpdx, dpdy, dpds;
+    for (R2* a : {&ufstar, &vfstar, &wfstar, &rhsp, &dpdx, &dpdy, &dpds}) a->init(NC, NZ);
+    predictor(c, ufstar, vfstar, wfstar);
     BCglobalVC(c, ufstar, vfstar, wfstar, c.ufv, c.vfv, c.wfv, 3);
     source3D(c, rhsp, ufstar, vfstar, wfstar);
 #pragma omp parallel for schedule(static)
@@ -1335,10 +1350,12 @@ int orc_step(orc_ctx* c, int fin_rk, orc_info* info) {
     // (known) = (n): nsmp3D.F90:419-441
     c->uf = c->ufn; c->vf = c->vfn; c->wf = c->wfn; c->pf = c->pfn;
     int nstage = (fin_rk == 3) ? 3 : (fin_rk == 2 ? 2 : 1);
-    int max_it = 0;
+    int max_it = 0, tot_it = 0, st_it[3] = {0, 0, 0};
     for (int s = 1; s <= nstage; ++s) {
         hydro(*c, fin_rk);
         max_it = std::max(max_it, c->info.iters);
+        tot_it += c->info.iters;
+        st_it[s - 1] = c->info.iters;
         if (fin_rk == 3 && s == 2) {
             // SSP-RK3 combination of cell velocities (extension)
             for (size_t q = 0; q < (size_t)NC * NZ; ++q) {
@@ -1366,7 +1383,12 @@ int orc_step(orc_ctx* c, int fin_rk, orc_info* info) {
     }
     // LoopTimeUpdate: (n) = (n+1)
     c->ufn = c->ufnp; c->vfn = c->vfnp; c->wfn = c->wfnp; c->pfn = c->pfnp;
-    if (info) { *info = c->info; info->iters = max_it; }
+    if (info) {
+        *info = c->info;
+        info->iters = max_it;
+        info->iters_total = tot_it;
+        for (int q = 0; q < 3; ++q) info->iters_stage[q] = st_it[q];
+    }
     return c->info.converged ? 0 : 1;
 }
 
@@ -1456,6 +1478,23 @@ int orc_apply_A(orc_ctx* c, const double* x, double* y) {
     return 0;
 }
 
+// The predictor u* of one stage from the level-n state (the known level is
+// set to level n first, as orc_step does); the AB2 history and flag are left
+// as they were.  (N_CELL,NZ) each.
+int orc_predictor(orc_ctx* c, double* us, double* vs, double* ws) {
+    set_threads(*c);
+    c->uf = c->ufn; c->vf = c->vfn; c->wf = c->wfn; c->pf = c->pfn;
+    const R2 hu = c->rhsuf, hv = c->rhsvf, hw = c->rhswf;
+    R2 a, b, d;
+    a.init(c->NC, c->NZ); b.init(c->NC, c->NZ); d.init(c->NC, c->NZ);
+    predictor(*c, a, b, d);
+    c->rhsuf = hu; c->rhsvf = hv; c->rhswf = hw;
+    std::memcpy(us, a.d.data(), a.d.size() * sizeof(double));
+    std::memcpy(vs, b.d.data(), b.d.size() * sizeof(double));
+    std::memcpy(ws, d.d.data(), d.d.size() * sizeof(double));
+    return 0;
+}
+
 int orc_gradient_lsm(orc_ctx* c, const double* f, double* dfdx, double* dfdy, double* dfds) {
     R2 fun, a, b, d;
     fun.init(c->NC, c->NZ); a.init(c->NC, c->NZ); b.init(c->NC, c->NZ); d.init(c->NC, c->NZ);
@@ -1481,28 +1520,169 @@ int orc_vertex_interp(orc_ctx* c, const double* f, int is_pressure, int tagBC, i
     return 0;
 }
 
-int orc_mass_diag(orc_ctx* c, double* out) {
+// glob_cfl: Main/cfl.F90:84-215, serial branch, on the level-n velocities
+// (nsmp3D.F90:604 calls it after LoopTimeUpdate) and the face fluxes.  One
+// running accumulator per quantity in the reference's loop order.  With
+// ref_bug_compat = 0 every flux is weighted by the cell height dsigv(k-1)
+// instead of dsig(k-1) (divergence) and dsig(k) (the rest).
+int orc_cfl_diag(orc_ctx* c, double* out) {
     const int N0 = c->N0, NZ = c->NZ;
-    double sabs = 0, smax = 0, ssum = 0, cfl = 0;
+    const bool compat = c->P.ref_bug_compat != 0;
+    auto hk = [&](int k) { return compat ? c->dsig(k) : c->dsigv(k - 1); };      // dsig(k)
+    auto hd = [&](int k) { return compat ? c->dsig(k - 1) : c->dsigv(k - 1); };  // dsig(k-1)
+    // velocity check (cfl.F90:84-113)
+    double umax = 0.0, vmax = 0.0, wmax = 0.0, sumu = 0.0, sumv = 0.0, sumw = 0.0;
     for (int k = 2; k <= NZ - 1; ++k)
         for (int i = 1; i <= N0; ++i) {
-            double dsv = c->dsigv(k - 1);
-            double flux = 0.0, fc = 0.0;
-            flux = flux + c->U1FACE(i, k) * c->dlVV(i, 1) * dsv;
-            flux = flux + c->U2FACE(i, k) * c->dlVV(i, 2) * dsv;
-            flux = flux + c->U3FACE(i, k) * c->dlVV(i, 3) * dsv;
+            if (std::fabs(c->ufn(i, k)) > std::fabs(umax)) umax = c->ufn(i, k);
+            if (std::fabs(c->vfn(i, k)) > std::fabs(vmax)) vmax = c->vfn(i, k);
+            if (std::fabs(c->wfn(i, k)) > std::fabs(wmax)) wmax = c->wfn(i, k);
+            sumu = c->ufn(i, k) * c->areaCell(i) * hk(k) + sumu;
+            sumv = c->vfn(i, k) * c->areaCell(i) * hk(k) + sumv;
+            sumw = c->wfn(i, k) * c->areaCell(i) * hk(k) + sumw;
+        }
+    // divergence-free check (cfl.F90:115-184)
+    double cfl = 0.0, flux_l = 0.0, flux_m = 0.0, flux_i = 0.0, flux_o = 0.0, flux_w = 0.0, sabs = 0.0;
+    for (int k = 2; k <= NZ - 1; ++k)
+        for (int i = 1; i <= N0; ++i) {
+            double flux = 0.0, flux_cfl = 0.0;
+            const double uface[3] = {c->U1FACE(i, k), c->U2FACE(i, k), c->U3FACE(i, k)};
+            for (int j = 1; j <= 3; ++j) {
+                flux = flux + uface[j - 1] * c->dlVV(i, j) * hd(k);
+                flux_cfl = flux_cfl + std::fabs(uface[j - 1] * c->dlVV(i, j) * hk(k));
+                const int jc = c->No_cp(i, j);
+                if (jc < 1 || jc > N0) flux_w = flux_w + uface[j - 1] * c->dlVV(i, j) * hk(k);
+            }
             flux = flux + c->UTFACE(i, k) * c->areaCell(i);
             flux = flux + c->UBFACE(i, k) * c->areaCell(i);
-            fc += std::fabs(c->U1FACE(i, k) * c->dlVV(i, 1) * dsv) + std::fabs(c->U2FACE(i, k) * c->dlVV(i, 2) * dsv) +
-                  std::fabs(c->U3FACE(i, k) * c->dlVV(i, 3) * dsv) + std::fabs(c->UBFACE(i, k) * c->areaCell(i)) +
-                  std::fabs(c->UTFACE(i, k) * c->areaCell(i));
-            fc = 0.5 * c->P.dt * fc / (c->areaCell(i) * dsv);
-            cfl = std::max(cfl, fc);
+            flux_cfl = flux_cfl + std::fabs(c->UBFACE(i, k) * c->areaCell(i)) +
+                       std::fabs(c->UTFACE(i, k) * c->areaCell(i));
+            flux_cfl = 0.5 * c->P.dt * flux_cfl / (c->areaCell(i) * hk(k));
+            if (flux_cfl > cfl) cfl = flux_cfl;
+            flux_l = flux_l + flux;
+            if (std::fabs(flux_m) < std::fabs(flux)) flux_m = flux;
+            if (k == 2 && c->bcbot == 1) flux_i = flux_i + c->UBFACE(i, k) * c->areaCell(i);
+            if (k == NZ - 1 && c->bctop == 1) flux_o = flux_o + c->UTFACE(i, k) * c->areaCell(i);
             sabs += std::fabs(flux);
-            smax = std::max(smax, std::fabs(flux));
-            ssum += flux;
         }
-    out[0] = sabs; out[1] = smax; out[2] = ssum; out[3] = cfl;
+    const double Vol = c->TotalVolume * (c->P.sigfin - c->P.sigini);  // cfl.F90:186
+    out[ORC_CFL_UMAX] = umax; out[ORC_CFL_VMAX] = vmax; out[ORC_CFL_WMAX] = wmax;
+    out[ORC_CFL_AVEU] = sumu / Vol; out[ORC_CFL_AVEV] = sumv / Vol; out[ORC_CFL_AVEW] = sumw / Vol;
+    out[ORC_CFL_MAX] = cfl;
+    out[ORC_CFL_FLUX_TOTAL] = flux_l;
+    out[ORC_CFL_FLUX_MAX] = flux_m;
+    out[ORC_CFL_FLUX_BC] = flux_i + flux_o + flux_w;  // cfl.F90:215
+    out[ORC_CFL_FLUX_BOT] = flux_i; out[ORC_CFL_FLUX_TOP] = flux_o; out[ORC_CFL_FLUX_SIDE] = flux_w;
+    out[ORC_CFL_ABS_DIV] = sabs;
+    return 0;
+}
+
+int orc_mass_diag(orc_ctx* c, double* out) {
+    double d[ORC_CFL_COUNT];
+    orc_cfl_diag(c, d);
+    out[0] = d[ORC_CFL_ABS_DIV];
+    out[1] = std::fabs(d[ORC_CFL_FLUX_MAX]);
+    out[2] = d[ORC_CFL_FLUX_TOTAL];
+    out[3] = d[ORC_CFL_MAX];
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Synthetic inputs, restated for the CPU baseline: the periodic jittered
+// triangle mesh in data.txt layout and the seeded channel initial state.
+// Neither exists in the reference (it ships no input decks).
+// ---------------------------------------------------------------------------
+
+// splitmix64 finaliser (Steele, Lea and Flood 2014) and a counter-based
+// uniform in [0,1) keyed by (seed, stream, index).
+static uint64_t orc_mix(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static double orc_u01(uint64_t seed, uint64_t stream, uint64_t index) {
+    const uint64_t h0 = orc_mix(orc_mix(seed) ^ orc_mix(stream * 0xD1B54A32D192ED03ull + 1) ^ index);
+    return (double)(orc_mix(h0 ^ index) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+int orc_mesh_generate(int nx, int ny, double x0, double x1, double y0, double y1, double jitter,
+                      unsigned long long seed, int* No_vp, int* No_cp, int* nbe, int* nbev, double* xv,
+                      double* yv) {
+    if (nx < 2 || ny < 2 || !(x1 > x0) || !(y1 > y0) || jitter < 0.0 || jitter > 0.3) return -1;
+    const int N0 = 2 * nx * ny, NV = (nx + 1) * (ny + 1);
+    const double hx = (x1 - x0) / nx, hy = (y1 - y0) / ny;
+    // vertices row by row; the box edges stay exact so periodic pairing by
+    // coordinate works; interior vertices move by up to jitter * spacing
+    for (int v = 0; v < NV; ++v) {
+        const int ix = v % (nx + 1), iy = v / (nx + 1);
+        const bool edge = ix == 0 || iy == 0 || ix == nx || iy == ny;
+        double x = (ix == nx) ? x1 : x0 + ix * hx;
+        double y = (iy == ny) ? y1 : y0 + iy * hy;
+        if (!edge) {
+            x += jitter * hx * (2.0 * orc_u01(seed, 1, 2ull * v) - 1.0);
+            y += jitter * hy * (2.0 * orc_u01(seed, 1, 2ull * v + 1) - 1.0);
+        }
+        xv[v] = x;
+        yv[v] = y;
+        nbev[v] = edge ? 1 : 0;
+    }
+    // two counter-clockwise triangles per quad, split along a seeded diagonal
+    for (int q = 0; q < nx * ny; ++q) {
+        const int ix = q % nx, iy = q / nx;
+        const int sw = 1 + ix + iy * (nx + 1), se = sw + 1, ne = se + (nx + 1), nw = sw + (nx + 1);
+        const bool ac = orc_u01(seed, 2, (uint64_t)q) < 0.5;
+        const int t[2][3] = {{sw, se, ac ? ne : nw}, {ac ? sw : se, ne, nw}};
+        for (int h = 0; h < 2; ++h)
+            for (int j = 0; j < 3; ++j) No_vp[2 * q + h + (size_t)j * N0] = t[h][j];
+    }
+    // neighbour across edge j (v_j -> v_j+1) is the triangle owning the
+    // reversed edge; 0 on the box boundary
+    std::vector<std::pair<uint64_t, int>> half((size_t)3 * N0);
+    auto key = [&](int a, int b) { return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b; };
+    for (int t = 0; t < N0; ++t)
+        for (int j = 0; j < 3; ++j)
+            half[(size_t)3 * t + j] = {key(No_vp[t + (size_t)j * N0], No_vp[t + (size_t)((j + 1) % 3) * N0]), t + 1};
+    std::sort(half.begin(), half.end());
+    for (int t = 0; t < N0; ++t) {
+        nbe[t] = 0;
+        for (int j = 0; j < 3; ++j) {
+            const uint64_t rev = key(No_vp[t + (size_t)((j + 1) % 3) * N0], No_vp[t + (size_t)j * N0]);
+            auto it = std::lower_bound(half.begin(), half.end(), std::make_pair(rev, 0));
+            const bool found = it != half.end() && it->first == rev;
+            No_cp[t + (size_t)j * N0] = found ? it->second : 0;
+            if (!found) nbe[t] = 1;
+        }
+    }
+    for (int t = 0; t < N0; ++t) {
+        const int a = No_vp[t] - 1, b = No_vp[t + N0] - 1, d = No_vp[t + 2 * (size_t)N0] - 1;
+        if (!((xv[b] - xv[a]) * (yv[d] - yv[a]) - (xv[d] - xv[a]) * (yv[b] - yv[a]) > 0.0)) return -2;
+    }
+    return 0;
+}
+
+// Channel state on the (N_CELL,NZ) grid: the reference's profile
+// umax z (2 - z) (Functions.F90:22-31) plus uniform noise of half-width amp
+// on u, v, w keyed by (seed, original cell, layer, component); p = 0 and
+// ghost entries 0.
+int orc_initial_channel(const orc_ctx* c, double umax, double amp, unsigned long long seed, double* u,
+                        double* v, double* w, double* p) {
+    const int NC = c->NC, NZ = c->NZ, N0 = c->N0;
+    std::fill(u, u + (size_t)NC * NZ, 0.0);
+    std::fill(v, v + (size_t)NC * NZ, 0.0);
+    std::fill(w, w + (size_t)NC * NZ, 0.0);
+    std::fill(p, p + (size_t)NC * NZ, 0.0);
+    for (int k = 1; k <= NZ; ++k) {
+        const double z = c->sig(k);
+        if (z < c->P.sigini || z > c->P.sigfin) continue;
+        for (int i = 1; i <= N0; ++i) {
+            const size_t q = (size_t)(i - 1) + (size_t)(k - 1) * NC;
+            const uint64_t cell_key = ((uint64_t)i << 20) ^ (uint64_t)k;
+            u[q] = umax * z * (2.0 - z) + amp * (2.0 * orc_u01(seed, 11, cell_key) - 1.0);
+            v[q] = amp * (2.0 * orc_u01(seed, 12, cell_key) - 1.0);
+            w[q] = amp * (2.0 * orc_u01(seed, 13, cell_key) - 1.0);
+        }
+    }
     return 0;
 }
 

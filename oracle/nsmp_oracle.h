@@ -45,6 +45,8 @@ typedef struct orc_info {
     double e2norm;      /* final relative L2 residual                */
     int converged;      /* 1 if min(e1,e2) < eps                     */
     double max_eddy;    /* max nu_t of the last stage (0 without LES)*/
+    int iters_total;    /* BiCGSTAB iterations of all stages of a step */
+    int iters_stage[3]; /* BiCGSTAB iterations of each stage of a step */
 } orc_info;
 
 typedef struct orc_ctx orc_ctx;
@@ -105,13 +107,29 @@ int orc_stats_sample(orc_ctx* c);                          /* glob_sample on lev
 int orc_stats_get(const orc_ctx* c, int which, double* out);  /* (N_CELL,NZ)       */
 int orc_stats_plane(const orc_ctx* c, double* out, double* tke); /* (NZ-2) x 10    */
 int orc_apply_A(orc_ctx* c, const double* x, double* y);   /* (N_CELL,NZ) -> (N0..)*/
+int orc_predictor(orc_ctx* c, double* us, double* vs, double* ws); /* u* of a stage from level n */
 int orc_gradient_lsm(orc_ctx* c, const double* f, double* dfdx, double* dfdy,
                      double* dfds);                         /* (N_CELL,NZ) each   */
 int orc_vertex_interp(orc_ctx* c, const double* f, int is_pressure, int tagBC,
                       int tagdir, double* fv);              /* cell -> vertex     */
-/* glob_cfl-style mass-flux diagnostics (cfl.F90:131-184): out[0] = sum |div|,
- * out[1] = max |div|, out[2] = sum div (signed), out[3] = max CFL. */
+/* glob_cfl (cfl.F90:84-215), out[ORC_CFL_COUNT] in the order of nsmp_cfl_diag. */
+enum {
+    ORC_CFL_UMAX = 0, ORC_CFL_VMAX, ORC_CFL_WMAX, ORC_CFL_AVEU, ORC_CFL_AVEV, ORC_CFL_AVEW,
+    ORC_CFL_MAX, ORC_CFL_FLUX_TOTAL, ORC_CFL_FLUX_MAX, ORC_CFL_FLUX_BC, ORC_CFL_FLUX_BOT,
+    ORC_CFL_FLUX_TOP, ORC_CFL_FLUX_SIDE, ORC_CFL_ABS_DIV, ORC_CFL_COUNT
+};
+int orc_cfl_diag(orc_ctx* c, double* out);
+/* out[0] = sum |div|, out[1] = max |div|, out[2] = sum div, out[3] = max CFL. */
 int orc_mass_diag(orc_ctx* c, double* out);
+
+/* Synthetic inputs (the oracle's own copy, for the CPU baseline): the
+ * periodic jittered mesh in data.txt layout and the seeded channel state on
+ * the (N_CELL,NZ) grid of a context. */
+int orc_mesh_generate(int nx, int ny, double x0, double x1, double y0, double y1, double jitter,
+                      unsigned long long seed, int* No_vp, int* No_cp, int* nbe, int* nbev,
+                      double* xv, double* yv);
+int orc_initial_channel(const orc_ctx* c, double umax, double amp, unsigned long long seed,
+                        double* u, double* v, double* w, double* p);
 
 #ifdef __cplusplus
 }

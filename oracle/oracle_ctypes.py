@@ -37,7 +37,15 @@ class OrcParams(C.Structure):
 
 class OrcInfo(C.Structure):
     _fields_ = [("iters", C.c_int), ("e1norm", C.c_double), ("e2norm", C.c_double),
-                ("converged", C.c_int), ("max_eddy", C.c_double)]
+                ("converged", C.c_int), ("max_eddy", C.c_double), ("iters_total", C.c_int),
+                ("iters_stage", C.c_int * 3)]
+
+
+# glob_cfl values (the order of nsmp_cfl_diag)
+CFL_NAMES = ["umax", "vmax", "wmax", "aveu", "avev", "avew", "cfl_max", "flux_total", "flux_max", "flux_bc",
+             "flux_bot", "flux_top", "flux_side", "abs_div"]
+
+PI_REF = 3.14159265359  # common.mpf:26
 
 
 _lib = None
@@ -71,14 +79,42 @@ def lib():
         L.orc_stats_get.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         L.orc_stats_plane.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_gradient_lsm.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+        L.orc_predictor.argtypes = [C.c_void_p] + [C.c_void_p] * 3
         L.orc_vertex_interp.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
         L.orc_mass_diag.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_cfl_diag.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_mesh_generate.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                        C.c_double, C.c_ulonglong] + [C.c_void_p] * 6
+        L.orc_initial_channel.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_ulonglong] + [C.c_void_p] * 4
         _lib = L
     return _lib
 
 
 def _ptr(a):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def channel_params(nx, ny, layers, dt, lx=2 * PI_REF, ly=PI_REF, height=2.0, re=180.0, les=1, les_van=1,
+                   grid_kind=1, beta=2.0, eps=1e-10, max_iters=10000, top_bc=0, bot_bc=0, ref_bug_compat=1):
+    """Oracle parameters of the periodic channel (2pi x pi x 2, tanh layers,
+    dp/dx = -1): the same values the product's channel parameters hold."""
+    return dict(n0=2 * nx * ny, nvert=(nx + 1) * (ny + 1), nz=layers + 2, xdini=0.0, xdfin=lx, ydini=0.0,
+                ydfin=ly, sigini=0.0, sigfin=height, grid_kind=grid_kind, grid_beta=beta, top_bc=top_bc,
+                bot_bc=bot_bc, dt=dt, re=re, bdx=1.0, bdy=0.0, bdz=0.0, eps=eps, max_iters=max_iters, les=les,
+                les_van=les_van, ref_bug_compat=ref_bug_compat)
+
+
+def make_mesh(nx, ny, lx=2 * PI_REF, ly=PI_REF, jitter=0.2, seed=0):
+    """The oracle's own periodic jittered mesh in data.txt layout."""
+    n0, nv = 2 * nx * ny, (nx + 1) * (ny + 1)
+    m = {"No_vp": np.zeros((n0, 3), np.int32, order="F"), "No_cp": np.zeros((n0, 3), np.int32, order="F"),
+         "nbe": np.zeros(n0, np.int32), "nbev": np.zeros(nv, np.int32),
+         "xv": np.zeros(nv, np.float64), "yv": np.zeros(nv, np.float64)}
+    rc = lib().orc_mesh_generate(nx, ny, 0.0, lx, 0.0, ly, jitter, seed,
+                                 *[_ptr(m[k]) for k in ("No_vp", "No_cp", "nbe", "nbev", "xv", "yv")])
+    if rc:
+        raise ValueError(f"orc_mesh_generate failed ({rc})")
+    return m
 
 
 class Oracle:
@@ -151,7 +187,8 @@ class Oracle:
         info = OrcInfo()
         rc = lib().orc_step(self.h, fin_rk, C.byref(info))
         return rc, {"iters": info.iters, "e1norm": info.e1norm, "e2norm": info.e2norm,
-                    "converged": info.converged, "max_eddy": info.max_eddy}
+                    "converged": info.converged, "max_eddy": info.max_eddy, "iters_total": info.iters_total,
+                    "iters_stage": list(info.iters_stage)}
 
     @property
     def flag_ab(self):
@@ -197,6 +234,12 @@ class Oracle:
         lib().orc_gradient_lsm(self.h, _ptr(f), *[_ptr(o) for o in outs])
         return outs
 
+    def predictor(self):
+        """u*, v*, w* of one stage from the level-n state (history untouched)."""
+        outs = [np.zeros((self.ncell, self.nz), order="F") for _ in range(3)]
+        lib().orc_predictor(self.h, *[_ptr(o) for o in outs])
+        return outs
+
     def vertex_interp(self, f, is_pressure=True, tag_bc=0, tagdir=2):
         f = np.asfortranarray(f, dtype=np.float64)
         out = np.zeros((self.nvert, self.nz - 1), dtype=np.float64, order="F")
@@ -207,3 +250,15 @@ class Oracle:
         out = np.zeros(4, dtype=np.float64)
         lib().orc_mass_diag(self.h, _ptr(out))
         return out
+
+    def cfl_diag(self):
+        """glob_cfl on the level-n state: dict of the CFL_NAMES values."""
+        out = np.zeros(len(CFL_NAMES), dtype=np.float64)
+        lib().orc_cfl_diag(self.h, _ptr(out))
+        return dict(zip(CFL_NAMES, out.tolist()))
+
+    def initial_channel(self, umax=18.0, amp=1.8, seed=1):
+        """The oracle's own seeded channel state on its (N_CELL,NZ) grid."""
+        arrs = [np.zeros((self.ncell, self.nz), np.float64, order="F") for _ in range(4)]
+        lib().orc_initial_channel(self.h, umax, amp, seed, *[_ptr(a) for a in arrs])
+        return arrs

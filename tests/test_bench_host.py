@@ -39,3 +39,25 @@ def test_roofline_of_the_fp64_solver_reports_its_fp64_rate():
     assert roof["algorithmic_bytes_per_launch"] == 8 * 8 * prisms
     flops = bench.FLOPS["k_bicg_x"] * prisms * iters
     assert math.isclose(roof["fp64_tflops"], round(flops / 0.0175 / 1e12, 3))
+
+
+def test_step_bytes_count_iterations_updates_and_stage_kernels():
+    prisms = 1000
+    prof = {"k_in_pv": (1100, 67.0), "k_in_st": (1100, 40.0), "k_mix_update": (300, 4.0),
+            "k_mix_scale": (300, 2.0), "k_stage_rhs": (6, 7.0), "k_project": (6, 3.0), "other": (4, 0.1),
+            "k_bicg_p": (0, 0.0)}
+    bstep, b_it, b_up, b_fix = bench.step_bytes(prof, iters=1000, updates=40, steps=2, prisms=prisms, mixed=True)
+    w = bench.WORDS_MIXED
+    assert b_it == (w["k_in_pv"] + w["k_in_st"]) * 8 * prisms
+    assert b_up == (w["k_mix_update"] + w["k_mix_scale"]) * 8 * prisms
+    assert b_fix == (bench.WORDS["k_stage_rhs"] * 6 + bench.WORDS["k_project"] * 6 + 3 * 4) * 8 * prisms / 2
+    assert math.isclose(bstep, b_fix + (b_it * 1000 + b_up * 40) / 2)
+
+
+def test_fp64_roofline_takes_the_lower_roof():
+    prisms, iters = 1048576, 500
+    prof = {"k_bicg_x": (500, 17.5)}
+    roof, _, _ = bench.roofline(prof, iters, prisms, mixed=False, fp64_peak=1.2)
+    assert roof["fp64_peak_tflops"] == 1.2
+    assert math.isclose(roof["fp64_frac"], round(roof["fp64_tflops"] / 1.2, 4))
+    assert roof["bound"] == ("fp64" if roof["fp64_frac"] > roof["frac"] else "hbm")

@@ -69,3 +69,20 @@ def test_reference_arm_two_ranks_rank0_only():
     assert d["impl"] == "reference" and d["n_gpus"] == 2
     assert d["value"] > 0 and d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] == "port"
+
+
+def test_reference_arm_loads_only_the_oracle():
+    """The CPU arm builds its workload from the oracle's own synthetic inputs
+    and never maps the product library."""
+    code = ("import sys, argparse, bench\n"
+            "a = argparse.Namespace(gpus=1, steps=1, warmup=1, workload='config0', ref_threads=2)\n"
+            "bench.run_reference(a)\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print('LOADED', 'libnsmpgpu' in maps, 'nsmp_gb300' in sys.modules, 'libnsmp_oracle' in maps)\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=REPO, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    last = [l for l in r.stdout.splitlines() if l.startswith("LOADED")][0]
+    assert last == "LOADED False False True", last
+    d = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][0])
+    assert d["steps"] == 1 and d["warmup"] == 1
+    assert len(d["bicgstab_iters_per_stage_timed"]) == 1 and len(d["bicgstab_iters_per_stage_timed"][0]) == 3
