@@ -14,8 +14,12 @@
 //   p = P2 A^+ P1 rhsp   (P1, P2 the Glob_Norm mean removals),
 // and A is symmetric, so its adjoint is the same BiCGSTAB solve applied to
 // the adjoint pressure (after the transposed mean removals).  Contributions
-// to neighbour cells and vertex classes are accumulated with FP64 atomics,
-// so the last bits of the gradient depend on the order in which blocks run.
+// to neighbour cells and vertex classes are not scattered with atomics: each
+// transposed kernel writes them to slot planes (one value per prism and kind
+// of contribution), and gather kernels add, for every destination, the slots
+// that point at it in a fixed order (lateral edges 0-2, the layer below, the
+// layer above; vertex classes over their incident corners in column order).
+// The gradient is therefore the same bit for bit from run to run.
 //
 // Memory: checkpoints of the state every `ckpt_every` steps and the PPE
 // solution of every stage (the pressure tape); during the reverse sweep one
@@ -49,6 +53,15 @@ struct AdjScratch {
     int* tptr = nullptr;    // transposed vertex stencil: cell -> (class, weight)
     int* tcls = nullptr;
     double* tcoef = nullptr;
+    // deterministic accumulation: a kernel writes each contribution to a
+    // neighbour into a slot plane (compact layout, one plane per kind of
+    // contribution); gather kernels then add, in a fixed order, the slots
+    // that point at each destination
+    double* slot = nullptr; // kSlotPlanes x nprism
+    int* nbrev = nullptr;   // (N0,3): edge of nb[c][j] that leads back to c
+    int* iptr = nullptr;    // vertex class -> incident (column, corner) pairs, column-major order
+    int* inc = nullptr;     //   encoded 3 * column + corner
+    bool pairing_ok = true; // every edge has exactly one reversed partner
     double tot_area = 0.0, hsum = 0.0;
     double seg_budget = 0.0;  // bytes for the segment's stage inputs; 0: 80 % of free memory
 };
@@ -57,6 +70,11 @@ namespace nsmp {
 namespace {
 
 constexpr int NF_STATE = 9;  // u, v, w, p + five face fluxes
+constexpr int kSlotPlanes = 24;  // k_adj_stage: 3 fields x (3 lateral + up + down + 3 corners)
+
+// Slot plane layout of one field's contributions: lateral across edge 0..2,
+// to the layer above, to the layer below; corner planes separately.
+enum { SL_L0 = 0, SL_UP = 3, SL_DN = 4, SL_CELL = 5 };
 
 // vertex values of u, v, w (the arithmetic of the forward k_vertex, so the
 // linearisation point is the forward's)
@@ -172,7 +190,12 @@ struct AdjProjArgs {
     double dt;
 };
 
-__global__ void __launch_bounds__(kBlock) k_adj_project(Mesh m, AdjProjArgs a) {
+// Contributions to other prisms go to slot planes 0-4 (lateral across edge
+// 0..2, above, below; zero at the walls) and the vertex-pressure
+// contributions per corner to planes 5-7; the prism's own part is added in
+// place.  k_gather_cells / k_gather_corners sum them in a fixed order.
+__global__ void __launch_bounds__(kBlock) k_adj_project(Mesh m, AdjProjArgs a, double* __restrict__ slot) {
+    const size_t np = (size_t)m.nprism;
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
         int c, k0;
         prism_of(m, g, c, k0);
@@ -182,27 +205,100 @@ __global__ void __launch_bounds__(kBlock) k_adj_project(Mesh m, AdjProjArgs a) {
         a.aus[q] = ub; a.avs[q] = vb; a.aws[q] = wb;
         const double Fb[3] = {a.f1[q], a.f2[q], a.f3[q]};
         double pc = a.ap[q];
+        double cv[3] = {0.0, 0.0, 0.0};
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             // d = p_nb - p enters dpdx, dpdy and the face correction dn_j
             const double t = -a.dt * (G.gx[j] * ub + G.gy[j] * vb + G.cA[j] * Fb[j]);
-            atomicAdd(a.apc + ICg(m, G.nb[j], k0), t);
+            slot[(SL_L0 + j) * np + g] = t;
             pc -= t;
             const double tv = -a.dt * G.cB[j] * Fb[j];   // (vb - va) * cB
-            atomicAdd(a.apv + IV(m, G.vtx[(j + 1) % 3], k0), tv);
-            atomicAdd(a.apv + IV(m, G.vtx[j], k0), -tv);
+            cv[(j + 1) % 3] += tv;
+            cv[j] -= tv;
         }
+        double up = 0.0, dn = 0.0;
         if (k0 < m.NZ - 2) {  // pT - p (zero at the top wall: Neumann ghost)
-            const double t = -a.dt * (lev(m, LV_GZP, k0) * wb + lev(m, LV_IDST, k0) * a.fT[q]);
-            atomicAdd(a.apc + g + 1, t);
-            pc -= t;
+            up = -a.dt * (lev(m, LV_GZP, k0) * wb + lev(m, LV_IDST, k0) * a.fT[q]);
+            pc -= up;
         }
         if (k0 > 1) {
-            const double t = -a.dt * (lev(m, LV_GZM, k0) * wb + lev(m, LV_IDSBU, k0) * a.fB[q]);
-            atomicAdd(a.apc + g - 1, t);
-            pc -= t;
+            dn = -a.dt * (lev(m, LV_GZM, k0) * wb + lev(m, LV_IDSBU, k0) * a.fB[q]);
+            pc -= dn;
         }
-        atomicAdd(a.apc + g, pc);
+        slot[SL_UP * np + g] = up;
+        slot[SL_DN * np + g] = dn;
+        a.apc[g] += pc;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) slot[(SL_CELL + j) * np + g] = cv[j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// deterministic gathers of the slot planes
+// ---------------------------------------------------------------------------
+// Per destination field: the planes of its lateral contributions (lat..lat+2,
+// indexed by the SOURCE's edge), of contributions from the layer below
+// (`up`, written by the prism below) and from the layer above (`dn`); -1:
+// none.  Cell-layout destinations also receive the wall-ghost entries
+// (folded into the interior later, as the forward's ghosts are copies).
+struct GatherArgs {
+    double* out[3];
+    int lat[3], up[3], dn[3];
+    int nf;
+};
+
+template <bool COMPACT>
+__global__ void __launch_bounds__(kBlock) k_gather_cells(Mesh m, const int* __restrict__ nbrev,
+                                                         const double* __restrict__ slot, GatherArgs ga) {
+    const size_t np = (size_t)m.nprism;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        int c, k0;
+        prism_of(m, g, c, k0);
+        const ColGeo& G = m.geo[c];
+        for (int f = 0; f < ga.nf; ++f) {
+            double s = 0.0;
+            if (ga.lat[f] >= 0)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                    s += slot[(size_t)(ga.lat[f] + __ldg(nbrev + 3 * c + j)) * np + ICg(m, G.nb[j], k0)];
+            if (ga.up[f] >= 0 && k0 > 1) s += slot[(size_t)ga.up[f] * np + g - 1];
+            if (ga.dn[f] >= 0 && k0 < m.NZ - 2) s += slot[(size_t)ga.dn[f] * np + g + 1];
+            double* o = ga.out[f];
+            if (COMPACT) {
+                o[g] += s;
+            } else {
+                o[IX(m, c, k0)] += s;
+                if (ga.dn[f] >= 0 && k0 == 1) o[IX(m, c, 0)] += slot[(size_t)ga.dn[f] * np + g];
+                if (ga.up[f] >= 0 && k0 == m.NZ - 2) o[IX(m, c, m.NZ - 1)] += slot[(size_t)ga.up[f] * np + g];
+            }
+        }
+    }
+}
+
+// Vertex classes: the corner planes base..base+2 of every (column, corner)
+// incident to the class, in ascending column order.
+struct CornerArgs {
+    double* out[3];
+    int base[3];
+    int nf;
+};
+
+__global__ void __launch_bounds__(kBlock) k_gather_corners(Mesh m, const int* __restrict__ iptr,
+                                                           const int* __restrict__ inc,
+                                                           const double* __restrict__ slot, CornerArgs ca) {
+    const size_t np = (size_t)m.nprism;
+    const int n = m.nclass * m.NZI;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int v = i / m.NZI, k0 = 1 + (i - v * m.NZI);
+        const int e0 = __ldg(iptr + v), e1 = __ldg(iptr + v + 1);
+        for (int f = 0; f < ca.nf; ++f) {
+            double s = 0.0;
+            for (int e = e0; e < e1; ++e) {
+                const int cj = __ldg(inc + e), cc = cj / 3, j = cj - 3 * cc;
+                s += slot[(size_t)(ca.base[f] + j) * np + ICg(m, cc, k0)];
+            }
+            ca.out[f][IV(m, v, k0)] += s;
+        }
     }
 }
 
@@ -289,7 +385,12 @@ struct AdjFaceArgs {
     double inv_dt;
 };
 
-__global__ void __launch_bounds__(kBlock) k_adj_faces(Mesh m, AdjFaceArgs a) {
+// Slot planes: u lateral 0-2, v lateral 3-5, w to the layer above 6 and
+// below 7, vertex-pressure corners 8-10; the prism's own parts in place.
+enum { SF_U = 0, SF_V = 3, SF_WUP = 6, SF_WDN = 7, SF_PC = 8 };
+
+__global__ void __launch_bounds__(kBlock) k_adj_faces(Mesh m, AdjFaceArgs a, double* __restrict__ slot) {
+    const size_t np = (size_t)m.nprism;
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
         int c, k0;
         prism_of(m, g, c, k0);
@@ -301,23 +402,25 @@ __global__ void __launch_bounds__(kBlock) k_adj_faces(Mesh m, AdjFaceArgs a) {
                               a.f3[q] + rb * G.L[2] * dsv * a.inv_dt};
         const double FTb = a.fT[q] + rb * G.area * a.inv_dt, FBb = a.fB[q] + rb * G.area * a.inv_dt;
         double ou = 0.0, ov = 0.0;
+        double cp[3] = {0.0, 0.0, 0.0};
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const size_t qn = IX(m, G.nb[j], k0);
             const double tu = 0.5 * G.xn[j] * Fb[j], tv = 0.5 * G.yn[j] * Fb[j];
-            atomicAdd(a.aus + qn, tu);
-            atomicAdd(a.avs + qn, tv);
+            slot[(SF_U + j) * np + g] = tu;
+            slot[(SF_V + j) * np + g] = tv;
             ou += tu;
             ov += tv;
             const double tp = -dsv * G.dle2[j] * rb;   // (pb - pa) * dle2, pb = vertex j+1
-            atomicAdd(a.apv + IV(m, G.vtx[(j + 1) % 3], k0), tp);
-            atomicAdd(a.apv + IV(m, G.vtx[j], k0), -tp);
+            cp[(j + 1) % 3] += tp;
+            cp[j] -= tp;
         }
-        atomicAdd(a.aus + q, ou);
-        atomicAdd(a.avs + q, ov);
-        atomicAdd(a.aws + q, 0.5 * FTb - 0.5 * FBb);
-        atomicAdd(a.aws + q + 1, 0.5 * FTb);
-        atomicAdd(a.aws + q - 1, -0.5 * FBb);
+        a.aus[q] += ou;
+        a.avs[q] += ov;
+        a.aws[q] += 0.5 * FTb - 0.5 * FBb;
+        slot[SF_WUP * np + g] = 0.5 * FTb;
+        slot[SF_WDN * np + g] = -0.5 * FBb;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) slot[(SF_PC + j) * np + g] = cp[j];
     }
 }
 
@@ -331,9 +434,9 @@ struct AdjStageArgs {
     const double *f1, *f2, *f3, *fT, *fB; // input face fluxes
     const double *aus, *avs, *aws;        // adjoint of u* (ghosts folded)
     double *au, *av, *aw;                 // adjoint of the input (accumulated, cell layout with ghosts)
-    double *auv, *avv, *awv;              // adjoint of the vertex values (class layout, accumulated)
     double *af1, *af2, *af3, *afT, *afB;  // adjoint of the input face fluxes (written)
     double* afx;                          // dJ/df_x (accumulated)
+    double* slot;                         // contributions to other prisms and vertex classes
     double c1, dt, inv_re;
     int les, les_van;
 };
@@ -460,9 +563,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_stage(Mesh m, AdjStageArgs a) {
             FTb[2] += dwdzb * ihz; FBb[2] -= dwdzb * ihz;
         }
         double* AU[3] = {a.au, a.av, a.aw};
-        double* AV[3] = {a.auv, a.avv, a.awv};
+        const size_t np = (size_t)m.nprism;
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
+            double* sl = a.slot + (size_t)(8 * f) * np;  // field f: lateral 0-2, up 3, down 4, corners 5-7
             double own = usb[f];          // u* = u + dt * r
             double vb[3] = {0.0, 0.0, 0.0};
             const double s = sdb[f] * dsv;
@@ -471,7 +575,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_stage(Mesh m, AdjStageArgs a) {
                 const int jj = (j + 1) % 3;
                 // diffusion: (xn - x0) kA + (f_jj - f_j) dle2
                 const double tn = s * G.kA[j] + 0.5 * Ffb[f][j];
-                atomicAdd(AU[f] + qn[j], tn);
+                sl[(SL_L0 + j) * np + g] = tn;
                 own += -s * G.kA[j] + 0.5 * Ffb[f][j];
                 const double tv = s * G.dle2[j] + G.kE[j] * Ffb[f][j];
                 vb[jj] += tv;
@@ -480,11 +584,11 @@ __global__ void __launch_bounds__(kBlock) k_adj_stage(Mesh m, AdjStageArgs a) {
             const double tT = sdb[f] * ar * idsT + 0.5 * FTb[f];
             const double tB = sdb[f] * ar * idsB + 0.5 * FBb[f];
             own += -sdb[f] * ar * idsT - sdb[f] * ar * idsB + 0.5 * FTb[f] + 0.5 * FBb[f];
-            atomicAdd(AU[f] + q + 1, tT);
-            atomicAdd(AU[f] + q - 1, tB);
-            atomicAdd(AU[f] + q, own);
+            sl[SL_UP * np + g] = tT;
+            sl[SL_DN * np + g] = tB;
+            AU[f][q] += own;
 #pragma unroll
-            for (int j = 0; j < 3; ++j) atomicAdd(AV[f] + qv[j], vb[j]);
+            for (int j = 0; j < 3; ++j) sl[(SL_CELL + j) * np + g] = vb[j];
         }
     }
 }
@@ -580,6 +684,38 @@ int adj_alloc(nsmp_ctx* c) {
     CK(cudaMemcpyAsync(S.tptr, tptr.data(), sizeof(int) * tptr.size(), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(S.tcls, tcls.data(), sizeof(int) * tcls.size(), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(S.tcoef, tcoef.data(), sizeof(double) * tcoef.size(), cudaMemcpyHostToDevice, c->stream));
+    // edge pairing of the gathers: edge j of column c runs from vertex class
+    // vtx[j] to vtx[j+1]; its neighbour n holds the same edge reversed
+    std::vector<int> nbrev(3 * (size_t)L.N0, -1);
+    for (int q = 0; q < L.N0; ++q)
+        for (int j = 0; j < 3; ++j) {
+            const ColGeo& G = L.geo[q];
+            const ColGeo& H = L.geo[G.nb[j]];
+            int found = -1, count = 0;
+            for (int e = 0; e < 3; ++e)
+                if (H.nb[e] == q && H.vtx[e] == G.vtx[(j + 1) % 3] && H.vtx[(e + 1) % 3] == G.vtx[j]) {
+                    found = e;
+                    ++count;
+                }
+            if (count != 1) S.pairing_ok = false;  // nsmp_adjoint refuses such a mesh
+            nbrev[3 * (size_t)q + j] = count == 1 ? found : 0;
+        }
+    std::vector<int> iptr(L.nclass + 1, 0), inc(3 * (size_t)L.N0);
+    for (int q = 0; q < L.N0; ++q)
+        for (int j = 0; j < 3; ++j) iptr[L.geo[q].vtx[j] + 1] += 1;
+    for (int v = 0; v < L.nclass; ++v) iptr[v + 1] += iptr[v];
+    {
+        std::vector<int> fill(iptr.begin(), iptr.end() - 1);
+        for (int q = 0; q < L.N0; ++q)  // ascending column, then corner: a fixed order
+            for (int j = 0; j < 3; ++j) inc[fill[L.geo[q].vtx[j]]++] = 3 * q + j;
+    }
+    CK(dalloc((void**)&S.nbrev, sizeof(int) * nbrev.size()));
+    CK(dalloc((void**)&S.iptr, sizeof(int) * iptr.size()));
+    CK(dalloc((void**)&S.inc, sizeof(int) * inc.size()));
+    CK(dalloc((void**)&S.slot, sizeof(double) * kSlotPlanes * ncmp));
+    CK(cudaMemcpyAsync(S.nbrev, nbrev.data(), sizeof(int) * nbrev.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(S.iptr, iptr.data(), sizeof(int) * iptr.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(S.inc, inc.data(), sizeof(int) * inc.size(), cudaMemcpyHostToDevice, c->stream));
     double ta = 0.0, hs = 0.0;
     for (int q = 0; q < L.N0; ++q) {
         ta += L.ppe[q].area;
@@ -685,7 +821,13 @@ int adj_stage(nsmp_ctx* c, const double* in, double* const* Aout, double* const*
     AdjProjArgs pa{Aout[0], Aout[1], Aout[2], Aout[3], Aout[4], Aout[5], Aout[6], Aout[7], Aout[8],
                    S.aus[0], S.aus[1], S.aus[2], S.apc, S.avx[3], P.dt};
     for (int f = 0; f < 3; ++f) CK(cudaMemsetAsync(S.aus[f], 0, ncf * sizeof(double), st));
-    LAUNCH(NSMP_K_OTHER, k_adj_project<<<gp, kBlock, 0, st>>>(m, pa));
+    LAUNCH(NSMP_K_OTHER, k_adj_project<<<gp, kBlock, 0, st>>>(m, pa, S.slot));
+    {
+        GatherArgs ga{{S.apc, nullptr, nullptr}, {SL_L0, -1, -1}, {SL_UP, -1, -1}, {SL_DN, -1, -1}, 1};
+        LAUNCH(NSMP_K_OTHER, k_gather_cells<true><<<gp, kBlock, 0, st>>>(m, S.nbrev, S.slot, ga));
+        CornerArgs ca{{S.avx[3], nullptr, nullptr}, {SL_CELL, 0, 0}, 1};
+        LAUNCH(NSMP_K_OTHER, k_gather_corners<<<gv, kBlock, 0, st>>>(m, S.iptr, S.inc, S.slot, ca));
+    }
     LAUNCH(NSMP_K_OTHER, (k_adj_vertexT<1, true><<<gp, kBlock, 0, st>>>(m, S.tptr, S.tcls, S.tcoef, S.avx[3], nullptr,
                                                                         nullptr, S.apc, nullptr, nullptr)));
     CK(cudaMemsetAsync(S.avx[3], 0, nvx * sizeof(double), st));
@@ -712,7 +854,13 @@ int adj_stage(nsmp_ctx* c, const double* in, double* const* Aout, double* const*
     // face pass
     AdjFaceArgs fa{S.arhs, Aout[4], Aout[5], Aout[6], Aout[7], Aout[8], S.aus[0], S.aus[1], S.aus[2], S.avx[3],
                    1.0 / P.dt};
-    LAUNCH(NSMP_K_OTHER, k_adj_faces<<<gp, kBlock, 0, st>>>(m, fa));
+    LAUNCH(NSMP_K_OTHER, k_adj_faces<<<gp, kBlock, 0, st>>>(m, fa, S.slot));
+    {
+        GatherArgs ga{{S.aus[0], S.aus[1], S.aus[2]}, {SF_U, SF_V, -1}, {-1, -1, SF_WUP}, {-1, -1, SF_WDN}, 3};
+        LAUNCH(NSMP_K_OTHER, k_gather_cells<false><<<gp, kBlock, 0, st>>>(m, S.nbrev, S.slot, ga));
+        CornerArgs ca{{S.avx[3], nullptr, nullptr}, {SF_PC, 0, 0}, 1};
+        LAUNCH(NSMP_K_OTHER, k_gather_corners<<<gv, kBlock, 0, st>>>(m, S.iptr, S.inc, S.slot, ca));
+    }
     LAUNCH(NSMP_K_OTHER, k_adj_fold<<<gc, kBlock, 0, st>>>(m, S.aus[0], S.aus[1], S.aus[2], nullptr));
     // stage right-hand side
     AdjStageArgs sa;
@@ -721,12 +869,19 @@ int adj_stage(nsmp_ctx* c, const double* in, double* const* Aout, double* const*
     sa.f1 = F[0]; sa.f2 = F[1]; sa.f3 = F[2]; sa.fT = F[3]; sa.fB = F[4];
     sa.aus = S.aus[0]; sa.avs = S.aus[1]; sa.aws = S.aus[2];
     sa.au = Ain[0]; sa.av = Ain[1]; sa.aw = Ain[2];
-    sa.auv = S.avx[0]; sa.avv = S.avx[1]; sa.awv = S.avx[2];
+    sa.slot = S.slot;
     sa.af1 = Ain[4]; sa.af2 = Ain[5]; sa.af3 = Ain[6]; sa.afT = Ain[7]; sa.afB = Ain[8];
     sa.afx = S.afx;
     sa.c1 = 1.0; sa.dt = P.dt; sa.inv_re = 1.0 / P.re;
     sa.les = P.les; sa.les_van = P.les_van;
     LAUNCH(NSMP_K_OTHER, k_adj_stage<<<gp, kBlock, 0, st>>>(m, sa));
+    {
+        GatherArgs ga{{Ain[0], Ain[1], Ain[2]}, {SL_L0, 8 + SL_L0, 16 + SL_L0}, {SL_UP, 8 + SL_UP, 16 + SL_UP},
+                      {SL_DN, 8 + SL_DN, 16 + SL_DN}, 3};
+        LAUNCH(NSMP_K_OTHER, k_gather_cells<false><<<gp, kBlock, 0, st>>>(m, S.nbrev, S.slot, ga));
+        CornerArgs ca{{S.avx[0], S.avx[1], S.avx[2]}, {SL_CELL, 8 + SL_CELL, 16 + SL_CELL}, 3};
+        LAUNCH(NSMP_K_OTHER, k_gather_corners<<<gv, kBlock, 0, st>>>(m, S.iptr, S.inc, S.slot, ca));
+    }
     LAUNCH(NSMP_K_OTHER, k_adj_fold<<<gc, kBlock, 0, st>>>(m, Ain[0], Ain[1], Ain[2], nullptr));
     // vertex transposes: velocity vertex values and the vertex p of the input
     LAUNCH(NSMP_K_OTHER, (k_adj_vertexT<3, false><<<gp, kBlock, 0, st>>>(m, S.tptr, S.tcls, S.tcoef, S.avx[0],
@@ -815,6 +970,11 @@ int run_adjoint(nsmp_ctx* c, int nsteps, int ckpt_every, const double* fx, doubl
     int rc = adj_alloc(c);
     if (rc) return rc;
     AdjScratch& S = *c->adj;
+    if (!S.pairing_ok) {
+        c->err = "nsmp_adjoint: a column meets a neighbour over two periodic edges (mesh of fewer than 3 quads "
+                 "across); the transposed stencils cannot pair its edges";
+        return NSMP_ERR_MESH;
+    }
     const Mesh& m = c->mesh;
     cudaStream_t st = c->stream;
     const size_t ncf = (size_t)c->L.N0 * c->L.NZ;
