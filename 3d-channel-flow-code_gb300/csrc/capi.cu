@@ -31,11 +31,12 @@ int nsmp_create(const nsmp_params* prm, const nsmp_mesh* mesh, nsmp_ctx** out) {
     try {
         c->prm = *prm;
         c->device = prm->device;
-        if (prm->precision != NSMP_FP64 && prm->precision != NSMP_MIXED) {
+        if (prm->precision != NSMP_FP64 && prm->precision != NSMP_MIXED && prm->precision != NSMP_MIXED_F32) {
             delete c;
             return NSMP_ERR_ARG;
         }
-        c->precision = prm->precision;
+        c->precision = (prm->precision == NSMP_FP64) ? NSMP_FP64 : NSMP_MIXED;
+        c->stage32 = prm->precision == NSMP_MIXED_F32;
         // the setup makes the context's device current; the caller's
         // current device is given back when nsmp_create returns
         nsmp::DeviceGuard guard(c->device);
@@ -259,14 +260,25 @@ int nsmp_mass_diag(nsmp_ctx* c, double out[4]) {
 }
 
 int nsmp_set_precision(nsmp_ctx* c, int mode) {
-    if (!c || (mode != NSMP_FP64 && mode != NSMP_MIXED)) return NSMP_ERR_ARG;
+    if (!c || (mode != NSMP_FP64 && mode != NSMP_MIXED && mode != NSMP_MIXED_F32)) return NSMP_ERR_ARG;
     NSMP_DEVICE_GUARD(c);
-    if (mode == NSMP_MIXED && !c->b64) {
+    if (mode != NSMP_FP64 && !c->b64) {
         int rc = nsmp::mixed_alloc(c);
         if (rc) return rc;
     }
-    c->precision = mode;
+    if (mode == NSMP_MIXED_F32) {
+        int rc = nsmp::stage32_alloc(c);
+        if (rc) return rc;
+    }
+    c->precision = (mode == NSMP_FP64) ? NSMP_FP64 : NSMP_MIXED;
+    c->stage32 = mode == NSMP_MIXED_F32;
     c->prm.precision = mode;
+    return NSMP_OK;
+}
+
+int nsmp_set_fp64_spmv(nsmp_ctx* c, int matrix_free) {
+    if (!c || (matrix_free != 0 && matrix_free != 1)) return NSMP_ERR_ARG;
+    c->fp64_spmv_mf = matrix_free;
     return NSMP_OK;
 }
 

@@ -47,6 +47,9 @@ struct nsmp_ctx {
     // hand-over: per column {kA1..3, area}, per level {dsigv, aT, aB, 0}
     float *ddcol = nullptr, *ddlev = nullptr;
     nsmp::ColPPE32* d_ppe32 = nullptr;
+    nsmp::ColGeo32* d_geo32 = nullptr;  // FP32 stage tables (NSMP_MIXED_F32)
+    int stage32 = 0;              // 1: stage right-hand side in FP32 arithmetic
+    int fp64_spmv_mf = 0;         // 1: FP64 BiCGSTAB regenerates its couplings instead of reading them
     int l2_limit_set = 0;         // 1: this context raised the persisting-L2 limit (restored by the last such context)
     double inner_tol = 1e-1;      // FP32 residual reduction that triggers an FP64 update
     int inner_cap = 50;           // most FP32 iterations between two FP64 updates
@@ -99,6 +102,7 @@ int run_mass_diag_noalloc(nsmp_ctx* c, double out[4]);
 int run_download_pv(nsmp_ctx* c, double* host);
 int cuda_fail(nsmp_ctx* c, cudaError_t e, const char* where);
 int mixed_alloc(nsmp_ctx* c);
+int stage32_alloc(nsmp_ctx* c);
 int fp64_setup(nsmp_ctx* c);
 // FP64 pressure solve of one stage; on return *x_final points at the solution
 // (compact layout, before the Glob_Norm mean removal).

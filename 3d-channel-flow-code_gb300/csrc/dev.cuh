@@ -66,6 +66,8 @@ struct Mesh {
     const int* vcell;
     const double* vcoef;
     const double* lev;     // LV_COUNT x NZ
+    const ColGeo32* geo32; // FP32 copies for the FP32 stage arithmetic (null until used)
+    const float* levf;
     double sgn_bot[3], sgn_top[3];
     double tv_lsig;        // TotalVolume*(SigFin-SigIni)
 };

@@ -59,6 +59,16 @@ struct ColGeo {
     int orig;        // original (data.txt) cell number, 0-based
 };
 
+// FP32 copy of the ColGeo members the stage right-hand side reads (the FP32
+// stage arithmetic of the mixed form).
+struct ColGeo32 {
+    int nb[3];
+    int vtx[3];
+    float kA[3], dle2[3], kE[3], L[3];
+    float lxu[3], lyu[3], lxv[3], lyv[3];
+    float area, inv_area, cbrt_area, pad;
+};
+
 // Per-layer factors, indexed by k0 = 1..NZ-2 (entries 0 and NZ-1 unused).
 struct Levels {
     std::vector<double> dsv;     // dsigv(k-1)

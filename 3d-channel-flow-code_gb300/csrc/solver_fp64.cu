@@ -157,6 +157,60 @@ __global__ void __launch_bounds__(kBlock) k_bicg_spmv(Mesh m, KryArgs a, RedScra
     }
 }
 
+// The same product matrix-free: each coupling A_ij D^-1_j is regenerated from
+// the column's kA_j (or area), the layer factor and D^-1 of the neighbour,
+// with the operations k_scaled_coefs uses, so the result is bitwise that of
+// the stored form.  It moves 5 fewer FP64 words a prism and issues 10 more
+// FP64 multiplies (nsmp_set_fp64_spmv selects it).
+template <int MODE>
+__global__ void __launch_bounds__(kBlock) k_bicg_spmv_mf(Mesh m, KryArgs a, RedScratch rs, Scal* sc) {
+    pdl_enter();
+    if (sc->done) return;
+    const double* __restrict__ in = (MODE == 0) ? a.p : a.s;
+    double* __restrict__ out = (MODE == 0) ? a.v : a.t;
+    const double* __restrict__ id = a.invD;
+    const int NZI = m.NZI;
+    double part[2] = {0.0, 0.0};
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        const int c = g / NZI;
+        const int kk = g - c * NZI;  // k0 - 1
+        const int k0 = kk + 1;
+        const ColPPE& P = m.ppe[c];
+        const double dsv = lev(m, LV_DSV, k0);
+        const double x0 = in[g];
+        double o = x0;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int gn = g + (P.nb[j] - c) * NZI;
+            o = fma((P.kA[j] * dsv) * id[gn], in[gn], o);
+        }
+        if (kk < NZI - 1) o = fma((P.area * lev(m, LV_IDST, k0)) * id[g + 1], in[g + 1], o);
+        if (kk > 0) o = fma((P.area * lev(m, LV_IDSB, k0)) * id[g - 1], in[g - 1], o);
+        out[g] = o;
+        if (MODE == 0) {
+            part[0] = fma(a.r0[g], o, part[0]);
+        } else {
+            part[0] = fma(o, x0, part[0]);
+            part[1] = fma(o, o, part[1]);
+        }
+    }
+    if (MODE == 0) {
+        double p1[1] = {part[0]}, t1[1];
+        if (grid_reduce<1, false>(p1, rs, t1) && threadIdx.x == 0) {
+            sc->r0v = t1[0];
+            if (fabs(t1[0]) < 1.0e-30) { sc->done = 1; sc->status = NSMP_WARN_BREAKDOWN; }
+            else sc->alpha = sc->rho / t1[0];
+        }
+    } else {
+        double tot[2];
+        if (grid_reduce<2, false>(part, rs, tot) && threadIdx.x == 0) {
+            sc->ts = tot[0];
+            sc->tt = tot[1];
+            sc->omega = tot[0] / tot[1];
+        }
+    }
+}
+
 // update_sk (bicgstab.F90:1007-1041)
 __global__ void __launch_bounds__(kBlock) k_bicg_s(Mesh m, KryArgs a, const Scal* sc) {
     pdl_enter();
@@ -255,9 +309,10 @@ int run_pressure_fp64(nsmp_ctx* c, const double* pf, const double** x_final) {
                {c->ahat[0], c->ahat[1], c->ahat[2], c->ahat[3], c->ahat[4]}};
     const int g_init = grid_occ(c, k_bicg_init, m.nprism);
     const int g_p = grid_occ(c, k_bicg_p, (m.nprism + 1) / 2);
-    const int g_v = grid_occ(c, k_bicg_spmv<0>, m.nprism);
+    const bool mf = c->fp64_spmv_mf != 0;
+    const int g_v = mf ? grid_occ(c, k_bicg_spmv_mf<0>, m.nprism) : grid_occ(c, k_bicg_spmv<0>, m.nprism);
     const int g_s = grid_occ(c, k_bicg_s, (m.nprism + 1) / 2);
-    const int g_t = grid_occ(c, k_bicg_spmv<1>, m.nprism);
+    const int g_t = mf ? grid_occ(c, k_bicg_spmv_mf<1>, m.nprism) : grid_occ(c, k_bicg_spmv<1>, m.nprism);
     const int g_x = grid_occ(c, k_bicg_x, (m.nprism + 1) / 2);
     LAUNCH(NSMP_K_BICG_INIT, k_bicg_init<<<g_init, kBlock, 0, st>>>(m, ka, c->red, c->d_scal));
     CKL("k_bicg_init");
@@ -268,9 +323,11 @@ int run_pressure_fp64(nsmp_ctx* c, const double* pf, const double** x_final) {
     for (;;) {
         for (int it = 0; it < chunk; ++it) {
             LAUNCH(NSMP_K_BICG_P, CK(launch_pdl(k_bicg_p, g_p, st, m, ka, c->d_scal)));
-            LAUNCH(NSMP_K_BICG_SPMV_V, CK(launch_pdl(k_bicg_spmv<0>, g_v, st, m, ka, c->red, c->d_scal)));
+            if (mf) LAUNCH(NSMP_K_BICG_SPMV_V, CK(launch_pdl(k_bicg_spmv_mf<0>, g_v, st, m, ka, c->red, c->d_scal)));
+            else LAUNCH(NSMP_K_BICG_SPMV_V, CK(launch_pdl(k_bicg_spmv<0>, g_v, st, m, ka, c->red, c->d_scal)));
             LAUNCH(NSMP_K_BICG_S, CK(launch_pdl(k_bicg_s, g_s, st, m, ka, c->d_scal)));
-            LAUNCH(NSMP_K_BICG_SPMV_T, CK(launch_pdl(k_bicg_spmv<1>, g_t, st, m, ka, c->red, c->d_scal)));
+            if (mf) LAUNCH(NSMP_K_BICG_SPMV_T, CK(launch_pdl(k_bicg_spmv_mf<1>, g_t, st, m, ka, c->red, c->d_scal)));
+            else LAUNCH(NSMP_K_BICG_SPMV_T, CK(launch_pdl(k_bicg_spmv<1>, g_t, st, m, ka, c->red, c->d_scal)));
             LAUNCH(NSMP_K_BICG_X, CK(launch_pdl(k_bicg_x, g_x, st, m, ka, c->red, c->d_scal)));
         }
         CKL("bicgstab iteration");

@@ -66,23 +66,47 @@ struct StageArgs {
     int les, les_van;
 };
 
+// The arithmetic type R of the stage right-hand side: FP64 (the plain form)
+// or FP32 (the mixed form's flux, gradient and Smagorinsky arithmetic).  Its
+// column and level tables come in the same type; the state, the predictor
+// update and the AB2 history stay FP64 either way.
+template <typename R>
+struct StageTables;
+template <>
+struct StageTables<double> {
+    static __device__ __forceinline__ const ColGeo& col(const Mesh& m, int c) { return m.geo[c]; }
+    static __device__ __forceinline__ double lv(const Mesh& m, int row, int k0) { return lev(m, row, k0); }
+};
+template <>
+struct StageTables<float> {
+    static __device__ __forceinline__ const ColGeo32& col(const Mesh& m, int c) { return m.geo32[c]; }
+    static __device__ __forceinline__ float lv(const Mesh& m, int row, int k0) {
+        return __ldg(m.levf + row * m.NZ + k0);
+    }
+};
+
 // Kim-Choi face value (interpolationFace.F90:85-111).
-__device__ __forceinline__ double face_val(double phi, double phinb, double kE, double fa, double fb) {
-    return phinb * 0.5 + phi * 0.5 + kE * (fb - fa);
+template <typename R>
+__device__ __forceinline__ R face_val(R phi, R phinb, R kE, R fa, R fb) {
+    return phinb * R(0.5) + phi * R(0.5) + kE * (fb - fa);
 }
 
+template <typename R>
 __global__ void __launch_bounds__(kBlock) k_stage_rhs(Mesh m, StageArgs a, RedScratch rs, Scal* sc) {
+    using T = StageTables<R>;
+    const R half = R(0.5);
     double emax[1] = {0.0};
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
         int c, k0;
         prism_of(m, g, c, k0);
-        const ColGeo& G = m.geo[c];
+        const auto& G = T::col(m, c);
         const size_t q = IX(m, c, k0);
-        const double dsv = lev(m, LV_DSV, k0), idsT = lev(m, LV_IDST, k0), idsB = lev(m, LV_IDSB, k0);
-        const double u = a.u[q], v = a.v[q], w = a.w[q];
-        const double uT = a.u[q + 1], vT = a.v[q + 1], wT = a.w[q + 1];
-        const double uB = a.u[q - 1], vB = a.v[q - 1], wB = a.w[q - 1];
-        double unb[3], vnb[3], wnb[3], fu[3], fv[3], fw[3];
+        const R dsv = T::lv(m, LV_DSV, k0), idsT = T::lv(m, LV_IDST, k0), idsB = T::lv(m, LV_IDSB, k0);
+        const double u64 = a.u[q], v64 = a.v[q], w64 = a.w[q];
+        const R u = R(u64), v = R(v64), w = R(w64);
+        const R uT = R(a.u[q + 1]), vT = R(a.v[q + 1]), wT = R(a.w[q + 1]);
+        const R uB = R(a.u[q - 1]), vB = R(a.v[q - 1]), wB = R(a.w[q - 1]);
+        R unb[3], vnb[3], wnb[3], fu[3], fv[3], fw[3];
         int nb[3], vx[3];
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
@@ -92,53 +116,53 @@ __global__ void __launch_bounds__(kBlock) k_stage_rhs(Mesh m, StageArgs a, RedSc
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             const size_t qn = IX(m, nb[j], k0);
-            unb[j] = a.u[qn]; vnb[j] = a.v[qn]; wnb[j] = a.w[qn];
+            unb[j] = R(a.u[qn]); vnb[j] = R(a.v[qn]); wnb[j] = R(a.w[qn]);
             const size_t qv = IV(m, vx[j], k0);
-            fu[j] = a.uv[qv]; fv[j] = a.vv[qv]; fw[j] = a.wv[qv];
+            fu[j] = R(a.uv[qv]); fv[j] = R(a.vv[qv]); fw[j] = R(a.wv[qv]);
         }
         // face values of the three components (advection and LES gradient)
-        double Uf[3], Vf[3], Wf[3];
+        R Uf[3], Vf[3], Wf[3];
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             const int jj = (j + 1) % 3;
-            Uf[j] = face_val(u, unb[j], G.kE[j], fu[j], fu[jj]);
-            Vf[j] = face_val(v, vnb[j], G.kE[j], fv[j], fv[jj]);
-            Wf[j] = face_val(w, wnb[j], G.kE[j], fw[j], fw[jj]);
+            Uf[j] = face_val<R>(u, unb[j], G.kE[j], fu[j], fu[jj]);
+            Vf[j] = face_val<R>(v, vnb[j], G.kE[j], fv[j], fv[jj]);
+            Wf[j] = face_val<R>(w, wnb[j], G.kE[j], fw[j], fw[jj]);
         }
-        const double UT = 0.5 * (u + uT), UB = 0.5 * (u + uB);
-        const double VT = 0.5 * (v + vT), VB = 0.5 * (v + vB);
-        const double WT = 0.5 * (w + wT), WB = 0.5 * (w + wB);
+        const R UT = half * (u + uT), UB = half * (u + uB);
+        const R VT = half * (v + vT), VB = half * (v + vB);
+        const R WT = half * (w + wT), WB = half * (w + wB);
         // Smagorinsky eddy viscosity (sgm_les.F90:208-250 with fvm_gradient
         // sgm_les.F90:437-473 and van Driest/Mason damping sgdamp)
-        double gam = a.inv_re, nut = 0.0;
+        R gam = R(a.inv_re), nut = R(0);
         if (a.les) {
-            double dudx = 0, dudy = 0, dvdx = 0, dvdy = 0, dwdx = 0, dwdy = 0;
+            R dudx = 0, dudy = 0, dvdx = 0, dvdy = 0, dwdx = 0, dwdy = 0;
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
                 dudx += Uf[j] * G.lxu[j]; dudy += Uf[j] * G.lyu[j];
                 dvdx += Vf[j] * G.lxv[j]; dvdy += Vf[j] * G.lyv[j];
                 dwdx += Wf[j] * G.lxu[j]; dwdy += Wf[j] * G.lyu[j];
             }
-            const double ihz = lev(m, LV_IHZ, k0);
-            const double dudz = (UT - UB) * ihz, dvdz = (VT - VB) * ihz, dwdz = (WT - WB) * ihz;
-            const double sxy = 0.5 * (dudy + dvdx), sxz = 0.5 * (dudz + dwdx), syz = 0.5 * (dvdz + dwdy);
-            const double sij = sqrt(2.0 * (dudx * dudx + dvdy * dvdy + dwdz * dwdz) +
-                                    4.0 * (sxy * sxy + sxz * sxz + syz * syz));
-            const double dd = G.cbrt_area * lev(m, LV_DD, k0);
-            double lw = lev(m, LV_KD, k0), l2;
+            const R ihz = T::lv(m, LV_IHZ, k0);
+            const R dudz = (UT - UB) * ihz, dvdz = (VT - VB) * ihz, dwdz = (WT - WB) * ihz;
+            const R sxy = half * (dudy + dvdx), sxz = half * (dudz + dwdx), syz = half * (dvdz + dwdy);
+            const R sij = sqrt(R(2) * (dudx * dudx + dvdy * dvdy + dwdz * dwdz) +
+                               R(4) * (sxy * sxy + sxz * sxz + syz * syz));
+            const R dd = G.cbrt_area * T::lv(m, LV_DD, k0);
+            R lw = T::lv(m, LV_KD, k0), l2;
             if (a.les_van) {
                 if (lw > dd) lw = dd;
-                const double l = lw * lev(m, LV_DAMP, k0);
+                const R l = lw * T::lv(m, LV_DAMP, k0);
                 l2 = l * l;
             } else {
-                l2 = 1.0 / (1.0 / (dd * dd) + 1.0 / (lw * lw));
+                l2 = R(1) / (R(1) / (dd * dd) + R(1) / (lw * lw));
             }
             nut = l2 * sij;
-            gam = nut + a.inv_re;
-            emax[0] = fmax(emax[0], nut);
+            gam = nut + R(a.inv_re);
+            emax[0] = fmax(emax[0], double(nut));
         }
         // diffusion (diffusion3D.F90:110-191; the dle3 term is identically 0)
-        double su = 0.0, sv = 0.0, sw = 0.0;
+        R su = 0, sv = 0, sw = 0;
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             const int jj = (j + 1) % 3;
@@ -146,39 +170,47 @@ __global__ void __launch_bounds__(kBlock) k_stage_rhs(Mesh m, StageArgs a, RedSc
             sv += (vnb[j] - v) * G.kA[j] + (fv[jj] - fv[j]) * G.dle2[j];
             sw += (wnb[j] - w) * G.kA[j] + (fw[jj] - fw[j]) * G.dle2[j];
         }
-        const double ar = G.area;
+        const R ar = G.area;
         su = su * dsv + ((uT - u) * idsT + (uB - u) * idsB) * ar;
         sv = sv * dsv + ((vT - v) * idsT + (vB - v) * idsB) * ar;
         sw = sw * dsv + ((wT - w) * idsT + (wB - w) * idsB) * ar;
         // advection (advection3D.F90:112-284)
-        const double F1 = a.f1[q] * G.L[0] * dsv, F2 = a.f2[q] * G.L[1] * dsv, F3 = a.f3[q] * G.L[2] * dsv;
-        const double FT = a.fT[q] * ar, FB = a.fB[q] * ar;
-        const double au = Uf[0] * F1 + Uf[1] * F2 + Uf[2] * F3 + UT * FT + UB * FB;
-        const double av = Vf[0] * F1 + Vf[1] * F2 + Vf[2] * F3 + VT * FT + VB * FB;
-        const double aw = Wf[0] * F1 + Wf[1] * F2 + Wf[2] * F3 + WT * FT + WB * FB;
-        const double ivol = G.inv_area * lev(m, LV_IDSV, k0);
-        const double ru = (a.fx ? a.bdx + a.fx[q] : a.bdx) + gam * su * ivol - au * ivol;
-        const double rv = a.bdy + gam * sv * ivol - av * ivol;
-        const double rw = a.bdz + gam * sw * ivol - aw * ivol;
-        // predictor (hydro.F90:322-333)
+        const R F1 = R(a.f1[q]) * G.L[0] * dsv, F2 = R(a.f2[q]) * G.L[1] * dsv, F3 = R(a.f3[q]) * G.L[2] * dsv;
+        const R FT = R(a.fT[q]) * ar, FB = R(a.fB[q]) * ar;
+        const R au = Uf[0] * F1 + Uf[1] * F2 + Uf[2] * F3 + UT * FT + UB * FB;
+        const R av = Vf[0] * F1 + Vf[1] * F2 + Vf[2] * F3 + VT * FT + VB * FB;
+        const R aw = Wf[0] * F1 + Wf[1] * F2 + Wf[2] * F3 + WT * FT + WB * FB;
+        const R ivol = G.inv_area * T::lv(m, LV_IDSV, k0);
+        const double bu = a.fx ? a.bdx + a.fx[q] : a.bdx;
+        double ru, rv, rw;
+        if constexpr (sizeof(R) == sizeof(double)) {  // the reference's order: rhs = b + diffusion - advection
+            ru = bu + gam * su * ivol - au * ivol;
+            rv = a.bdy + gam * sv * ivol - av * ivol;
+            rw = a.bdz + gam * sw * ivol - aw * ivol;
+        } else {  // the O(1) forcing is added in FP64 to the FP32 flux balance
+            ru = bu + double(gam * su * ivol - au * ivol);
+            rv = a.bdy + double(gam * sv * ivol - av * ivol);
+            rw = a.bdz + double(gam * sw * ivol - aw * ivol);
+        }
+        // predictor (hydro.F90:322-333), FP64
         double pu = a.c1 * ru, pv = a.c1 * rv, pw = a.c1 * rw;
         if (a.c2 != 0.0) {
             pu += a.c2 * a.hu[q];
             pv += a.c2 * a.hv[q];
             pw += a.c2 * a.hw[q];
         }
-        const double us = u + a.dt * pu, vs = v + a.dt * pv, ws = w + a.dt * pw;
+        const double us = u64 + a.dt * pu, vs = v64 + a.dt * pv, ws = w64 + a.dt * pw;
         a.us[q] = us; a.vs[q] = vs; a.ws[q] = ws;
         a.hu[q] = ru; a.hv[q] = rv; a.hw[q] = rw;
-        if (a.les) a.eddy[q] = nut;
+        if (a.les) a.eddy[q] = double(nut);
         // wall ghost layers (BCvelcenter3D, BC.F90:459-527; BCpcenter for nu_t)
         if (k0 == 1) {
             a.us[q - 1] = m.sgn_bot[0] * us; a.vs[q - 1] = m.sgn_bot[1] * vs; a.ws[q - 1] = m.sgn_bot[2] * ws;
-            if (a.les) a.eddy[q - 1] = nut;
+            if (a.les) a.eddy[q - 1] = double(nut);
         }
         if (k0 == m.NZ - 2) {
             a.us[q + 1] = m.sgn_top[0] * us; a.vs[q + 1] = m.sgn_top[1] * vs; a.ws[q + 1] = m.sgn_top[2] * ws;
-            if (a.les) a.eddy[q + 1] = nut;
+            if (a.les) a.eddy[q + 1] = double(nut);
         }
     }
     if (a.les) {
@@ -514,7 +546,10 @@ int run_stage(nsmp_ctx* c, int fin_rk, nsmp_stage_info* info) {
     sa.dt = P.dt; sa.inv_re = 1.0 / P.re; sa.bdx = P.bdx; sa.bdy = P.bdy; sa.bdz = P.bdz;
     sa.les = P.les; sa.les_van = P.les_van;
     sa.fx = c->fx;
-    LAUNCH(NSMP_K_STAGE_RHS, k_stage_rhs<<<grid_occ(c, k_stage_rhs, m.nprism), kBlock, 0, st>>>(m, sa, c->red, c->d_scal));
+    if (c->stage32)
+        LAUNCH(NSMP_K_STAGE_RHS, k_stage_rhs<float><<<grid_occ(c, k_stage_rhs<float>, m.nprism), kBlock, 0, st>>>(m, sa, c->red, c->d_scal));
+    else
+        LAUNCH(NSMP_K_STAGE_RHS, k_stage_rhs<double><<<grid_occ(c, k_stage_rhs<double>, m.nprism), kBlock, 0, st>>>(m, sa, c->red, c->d_scal));
     CKL("k_stage_rhs");
     FaceArgs fa{c->ustar[0], c->ustar[1], c->ustar[2], c->vtx[3], c->face[0], c->face[1], c->face[2],
                 c->face[3], c->face[4], c->rhsp, 1.0 / P.dt, 1};
@@ -620,6 +655,58 @@ int run_scatter(nsmp_ctx* c, const double* host, double* dfield, int rows, bool 
     return 0;
 }
 
+// The per-layer factor table of the kernels (lev[row * NZ + k0]).
+std::vector<double> level_table(const HostLayout& L) {
+    std::vector<double> lv((size_t)LV_COUNT * L.NZ, 0.0);
+    const Levels& V = L.lev;
+    const std::vector<double>* rows[LV_COUNT] = {&V.dsv, nullptr, &V.idsT, &V.idsB, &V.idsBu, &V.wT, &V.wB,
+                                                 &V.gzp, &V.gzm, &V.hmean, &V.les_dd, &V.les_kd, &V.les_damp, &V.ihz,
+                                                 nullptr, nullptr, &V.cfl_div, &V.cfl_h};
+    for (int r = 0; r < LV_COUNT; ++r)
+        for (int k = 0; k < L.NZ; ++k) {
+            double val;
+            if (r == LV_IDSV) val = (V.dsv[k] != 0.0) ? 1.0 / V.dsv[k] : 0.0;
+            else if (r == LV_ATOP) val = V.idsT[k] * V.wT[k];  // PPE coupling / area to the layer above
+            else if (r == LV_ABOT) val = V.idsB[k] * V.wB[k];  // and below (0 at the walls)
+            else val = (*rows[r])[k];
+            lv[(size_t)r * L.NZ + k] = val;
+        }
+    return lv;
+}
+
+// FP32 column and level tables of the FP32 stage arithmetic, once.
+int stage32_alloc(nsmp_ctx* c) {
+    if (c->d_geo32) return 0;
+    const HostLayout& L = c->L;
+    std::vector<ColGeo32> g32(L.N0);
+    for (int q = 0; q < L.N0; ++q) {
+        const ColGeo& G = L.geo[q];
+        ColGeo32& H = g32[q];
+        for (int j = 0; j < 3; ++j) {
+            H.nb[j] = G.nb[j]; H.vtx[j] = G.vtx[j];
+            H.kA[j] = (float)G.kA[j]; H.dle2[j] = (float)G.dle2[j]; H.kE[j] = (float)G.kE[j]; H.L[j] = (float)G.L[j];
+            H.lxu[j] = (float)G.lxu[j]; H.lyu[j] = (float)G.lyu[j];
+            H.lxv[j] = (float)G.lxv[j]; H.lyv[j] = (float)G.lyv[j];
+        }
+        H.area = (float)G.area; H.inv_area = (float)G.inv_area; H.cbrt_area = (float)G.cbrt_area; H.pad = 0.f;
+    }
+    const std::vector<double> lv = level_table(L);
+    std::vector<float> lvf(lv.begin(), lv.end());
+    ColGeo32* dg = nullptr;
+    float* dl = nullptr;
+    CK(cudaMalloc((void**)&dg, sizeof(ColGeo32) * g32.size()));
+    c->allocs.push_back(dg);
+    CK(cudaMalloc((void**)&dl, sizeof(float) * lvf.size()));
+    c->allocs.push_back(dl);
+    CK(cudaMemcpyAsync(dg, g32.data(), sizeof(ColGeo32) * g32.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(dl, lvf.data(), sizeof(float) * lvf.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->d_geo32 = dg;
+    c->mesh.geo32 = dg;
+    c->mesh.levf = dl;
+    return 0;
+}
+
 int ctx_init_device(nsmp_ctx* c) {
     CK(cudaSetDevice(c->device));
     CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
@@ -673,20 +760,7 @@ int ctx_init_device(nsmp_ctx* c) {
     CK(cudaMemcpyAsync(c->d_vptr, L.vptr.data(), sizeof(int) * L.vptr.size(), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->d_vcell, L.vcell.data(), sizeof(int) * L.vcell.size(), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->d_vcoef, L.vcoef.data(), sizeof(double) * L.vcoef.size(), cudaMemcpyHostToDevice, c->stream));
-    std::vector<double> lv((size_t)LV_COUNT * L.NZ, 0.0);
-    const Levels& V = L.lev;
-    const std::vector<double>* rows[LV_COUNT] = {&V.dsv, nullptr, &V.idsT, &V.idsB, &V.idsBu, &V.wT, &V.wB,
-                                                 &V.gzp, &V.gzm, &V.hmean, &V.les_dd, &V.les_kd, &V.les_damp, &V.ihz,
-                                                 nullptr, nullptr, &V.cfl_div, &V.cfl_h};
-    for (int r = 0; r < LV_COUNT; ++r)
-        for (int k = 0; k < L.NZ; ++k) {
-            double val;
-            if (r == LV_IDSV) val = (V.dsv[k] != 0.0) ? 1.0 / V.dsv[k] : 0.0;
-            else if (r == LV_ATOP) val = V.idsT[k] * V.wT[k];  // PPE coupling / area to the layer above
-            else if (r == LV_ABOT) val = V.idsB[k] * V.wB[k];  // and below (0 at the walls)
-            else val = (*rows[r])[k];
-            lv[(size_t)r * L.NZ + k] = val;
-        }
+    const std::vector<double> lv = level_table(L);
     CK(cudaMemcpyAsync(c->d_lev, lv.data(), sizeof(double) * lv.size(), cudaMemcpyHostToDevice, c->stream));
     std::vector<int> gcol(L.NC), vg(L.NV);
     for (int i = 0; i < L.NC; ++i) gcol[i] = (i < L.N0) ? L.iperm[i] : L.iperm[L.ghost_img[i - L.N0]];
@@ -705,13 +779,19 @@ int ctx_init_device(nsmp_ctx* c) {
         int rc = fp64_setup(c);
         if (rc) return rc;
     }
+    m.geo32 = nullptr;
+    m.levf = nullptr;
     Scal s0{};
     s0.eps = c->prm.eps;
     s0.max_iters = c->prm.max_iters;
     s0.inner_tol = c->inner_tol;
     CK(cudaMemcpyAsync(c->d_scal, &s0, sizeof(Scal), cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    if (c->precision == NSMP_MIXED) return mixed_alloc(c);
+    if (c->precision == NSMP_MIXED) {
+        int rc = mixed_alloc(c);
+        if (rc) return rc;
+    }
+    if (c->stage32) return stage32_alloc(c);
     return 0;
 }
 

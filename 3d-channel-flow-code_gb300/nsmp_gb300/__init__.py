@@ -18,7 +18,7 @@ PI_REF = 3.14159265359  # common.mpf:26
 # status codes (include/nsmp.h)
 OK, WARN_MAXITER, WARN_BREAKDOWN = 0, 1, 2
 ERR_ARG, ERR_MESH, ERR_CUDA, ERR_NAN, ERR_UNSUPPORTED, ERR_NOMEM, ERR_RANGE = -1, -2, -3, -4, -5, -6, -7
-FP64, MIXED = 0, 1
+FP64, MIXED, MIXED_F32 = 0, 1, 2
 
 (F_U, F_V, F_W, F_P, F_U1FACE, F_U2FACE, F_U3FACE, F_UTFACE, F_UBFACE, F_RHSU, F_RHSV,
  F_RHSW, F_EDDY, F_UNP, F_VNP, F_WNP, F_PNP, F_PV) = range(18)
@@ -66,7 +66,7 @@ EXPORTS = [
     "nsmp_set_body_force", "nsmp_wall_shear", "nsmp_adjoint", "nsmp_apply_A", "nsmp_apply_AT",
     "nsmp_set_adjoint_budget", "nsmp_stats_reset", "nsmp_stats_sample", "nsmp_stats_count",
     "nsmp_stats_download", "nsmp_stats_plane", "nsmp_download_vertex", "nsmp_cfl_diag",
-    "nsmp_solver_counters", "nsmp_probe_fp64_fma",
+    "nsmp_solver_counters", "nsmp_probe_fp64_fma", "nsmp_set_fp64_spmv",
 ]
 
 # glob_cfl values of nsmp_cfl_diag (NSMP_CFL_* order)
@@ -146,6 +146,7 @@ def lib(build_if_missing=True):
     L.nsmp_counters.argtypes = [vp, P(C.c_longlong), P(C.c_longlong)]
     L.nsmp_solver_log.argtypes = [vp, C.c_int, vp, vp, vp, vp]
     L.nsmp_solver_counters.argtypes = [vp, P(C.c_longlong), P(C.c_longlong)]
+    L.nsmp_set_fp64_spmv.argtypes = [vp, C.c_int]
     L.nsmp_probe_fp64_fma.argtypes = [C.c_int, C.c_int, P(C.c_double), P(C.c_double)]
     _lib = L
     return L
@@ -435,6 +436,10 @@ class Solver:
     @property
     def stream(self):
         return self.L.nsmp_stream(self.h)
+
+    def set_fp64_spmv(self, matrix_free):
+        """FP64 solver couplings: stored (False) or regenerated matrix-free (True)."""
+        self._check(self.L.nsmp_set_fp64_spmv(self.h, 1 if matrix_free else 0))
 
     def set_precision(self, mode):
         self._check(self.L.nsmp_set_precision(self.h, int(mode)))

@@ -52,6 +52,10 @@ WORDS = {
 FLOPS = {"k_bicg_spmv_v": 33, "k_bicg_spmv_t": 34, "k_bicg_x": 13, "k_bicg_p": 4, "k_bicg_s": 2}
 
 
+# bench precision names -> the library's precision modes
+PRECISIONS = {"fp64": lambda ng: ng.FP64, "mixed": lambda ng: ng.MIXED, "mixed_f32": lambda ng: ng.MIXED_F32}
+
+
 def load_peaks():
     path = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -396,15 +400,17 @@ def run_ours(args):
     nx, ny, layers, dt = WORKLOADS[args.workload]
     prisms = 2 * nx * ny * layers
     mesh = ng.make_mesh(nx, ny)
-    precs = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
-    head = "mixed" if "mixed" in precs else precs[0]
+    precs = ["fp64", args.mixed_form] if args.precision == "both" else [args.precision]
+    head = precs[-1]
     res, solvers = {}, {}
     snap = u_end = None
     fp64_peak, _ = ng.probe_fp64_fma(local)
     for prec in precs:
         prm = ng.channel_params(nx, ny, layers, dt, device=local,
-                                precision=(ng.MIXED if prec == "mixed" else ng.FP64))
+                                precision=PRECISIONS[prec](ng))
         s = ng.Solver(prm, mesh)
+        if prec == "fp64" and args.fp64_spmv == "matrix-free":
+            s.set_fp64_spmv(True)
         u0, v0, w0, p0 = ng.initial_channel(prm, s.ncell, seed=1)
         s.user_initial(u0, v0, w0, p0)
         stream = torch.cuda.ExternalStream(s.stream)
@@ -424,12 +430,12 @@ def run_ours(args):
         # per-kernel device times over K further steps of the same run
         rp = timed_region(s, ng, torch, stream, args.steps, pg, local, profile=True)
         r["prof"], r["prof_ms"], r["prof_iters"] = rp["prof"], rp["ms"], rp["iters"]
-        r["roof"], r["shares"], r["busy_ms"] = roofline(rp["prof"], rp["iters"], prisms, prec == "mixed",
+        r["roof"], r["shares"], r["busy_ms"] = roofline(rp["prof"], rp["iters"], prisms, prec != "fp64",
                                                         fp64_peak)
         # whole step: the timed region's iterations and FP64 updates with the
         # per-kernel bytes of the profiled region
         _, b_it, b_up, b_fix = step_bytes(rp["prof"], rp["iters"], rp["updates"], args.steps, prisms,
-                                          prec == "mixed")
+                                          prec != "fp64")
         bstep = b_fix + (b_it * r["iters"] + b_up * r["updates"]) / args.steps
         hbm_peak, _ = load_peaks()
         r["roof"]["step_bytes"] = bstep
@@ -452,14 +458,15 @@ def run_ours(args):
     # mixed vs FP64 after the same W + K steps from the same initial state
     cmp = None
     if len(res) == 2:
-        a, b = solvers["mixed"][0], solvers["fp64"][0]
+        a, b = solvers[head][0], solvers["fp64"][0]
         n0 = prm["n0"]
         cmp = {f"rel_l2_{nm}": float(np.linalg.norm(a.download(f)[:n0, 1:-1] - b.download(f)[:n0, 1:-1]) /
                                      np.linalg.norm(b.download(f)[:n0, 1:-1]))
                for nm, f in (("u", ng.F_U), ("v", ng.F_V), ("w", ng.F_W), ("p", ng.F_P))}
         da, db = a.mass_diag(), b.mass_diag()
         cmp["max_div_mixed"], cmp["max_div_fp64"] = float(da[1]), float(db[1])
-        cmp["speedup"] = res["mixed"]["value"] / res["fp64"]["value"]
+        cmp["speedup"] = res[head]["value"] / res["fp64"]["value"]
+        cmp["mixed_form"] = head
         cmp["after_steps"] = args.warmup + 2 * args.steps
 
     # ---- end to end: the timed steps replayed through the C-ABI -------------
@@ -501,7 +508,7 @@ def run_ours(args):
             "metric": "Mcell-steps/s", "value": r["value"], "unit": "Mcell-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_max"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+f64" if head == "mixed" else "f64",
+            "dtype": "f64" if head == "fp64" else "f32+f64",
             "data": "synthetic (seeded mesh and initial state; no dataset exists for this path)",
             "config": {"workload": workload_desc(args.workload), "prisms": prisms, "precision": head,
                        "integrator": "SSP-RK3 of the reference stage",
@@ -522,7 +529,7 @@ def run_ours(args):
         }
         if "fp64" in res and head != "fp64":
             f = res["fp64"]
-            line["fp64"] = {"value": f["value"], "ms_per_step": f["ms_max"] / args.steps,
+            line["fp64"] = {"value": f["value"], "ms_per_step": f["ms_max"] / args.steps, "spmv": args.fp64_spmv,
                             "bicgstab_iters_per_stage": round(f["iters"] / (3.0 * args.steps), 1),
                             "roofline": f["roof"], "kernel_share": f["shares"], "gpu_launches": f["launches"],
                             "clocks": f["clocks"]}
@@ -537,39 +544,55 @@ def run_ours(args):
 
 
 def run_accuracy(args):
-    """Mixed vs FP64 after N RK3 steps from the same initial state: relative
-    L2 of u, v, w, p over the interior and the max |div| of each run."""
+    """Mixed forms vs FP64 after N RK3 steps from the same initial state:
+    relative L2 of u, v, w, p over the interior and glob_cfl of each run
+    (max |div| is the reference's "Maxim flux").  Arms: FP64; mixed (FP32
+    Krylov + FP64 refinement, FP64 stage); mixed_f32 (the same with the stage
+    right-hand side in FP32); and, with --accuracy-compat0, the mixed form
+    with the reference's quirks corrected (ref_bug_compat = 0)."""
     import nsmp_gb300 as ng
 
     nx, ny, layers, dt = WORKLOADS[args.workload]
     mesh = ng.make_mesh(nx, ny)
+    arms = [("fp64", ng.FP64, 1), ("mixed", ng.MIXED, 1), ("mixed_f32", ng.MIXED_F32, 1)]
+    if args.accuracy_compat0:
+        arms.append(("mixed_compat0", ng.MIXED, 0))
     sol = {}
     clocks = ClockSampler(0)
     clocks.start()
-    for prec in ("fp64", "mixed"):
-        prm = ng.channel_params(nx, ny, layers, dt, precision=(ng.MIXED if prec == "mixed" else ng.FP64))
+    for name, prec, compat in arms:
+        prm = ng.channel_params(nx, ny, layers, dt, precision=prec, ref_bug_compat=compat)
         s = ng.Solver(prm, mesh)
         u0, v0, w0, p0 = ng.initial_channel(prm, s.ncell, seed=1)
         s.user_initial(u0, v0, w0, p0)
         worst = 0
+        it0, _ = s.solver_counters()
         t0 = time.perf_counter()
         for _ in range(args.accuracy_steps):
             rc, _ = s.step(3, 1)
             worst = max(worst, rc)
-        sol[prec] = {"fields": {nm: s.download(f)[:prm["n0"], 1:-1] for nm, f in
+        wall = time.perf_counter() - t0
+        it1, _ = s.solver_counters()
+        sol[name] = {"fields": {nm: s.download(f)[:prm["n0"], 1:-1] for nm, f in
                                 (("u", ng.F_U), ("v", ng.F_V), ("w", ng.F_W), ("p", ng.F_P))},
-                     "div": s.mass_diag(), "cfl": s.cfl_diag(), "status": worst, "s": time.perf_counter() - t0}
+                     "cfl": s.cfl_diag(), "status": worst, "s": wall,
+                     "its_per_stage": (it1 - it0) / (3.0 * max(args.accuracy_steps, 1))}
         s.close()
-    a, b = sol["mixed"], sol["fp64"]
-    out = {"accuracy": "mixed vs fp64", "workload": workload_desc(args.workload), "steps": args.accuracy_steps}
-    for nm in ("u", "v", "w", "p"):
-        out[f"rel_l2_{nm}"] = float(np.linalg.norm(a["fields"][nm] - b["fields"][nm]) / np.linalg.norm(b["fields"][nm]))
-    out["max_div_mixed"], out["max_div_fp64"] = float(a["div"][1]), float(b["div"][1])
-    out["max_div_diff"] = abs(out["max_div_mixed"] - out["max_div_fp64"])
-    out["status"] = {"mixed": a["status"], "fp64": b["status"]}
-    out["wall_s"] = {"mixed": round(a["s"], 1), "fp64": round(b["s"], 1)}
-    out["clocks"] = clocks.stop()
-    out["cfl_mixed"], out["cfl_fp64"] = a["cfl"], b["cfl"]
+    clk = clocks.stop()
+    b = sol["fp64"]
+    out = {"accuracy": "mixed forms vs fp64", "workload": workload_desc(args.workload),
+           "steps": args.accuracy_steps}
+    for name in sol:
+        a = sol[name]
+        d = {"status": a["status"], "wall_s": round(a["s"], 1), "bicgstab_iters_per_stage": round(a["its_per_stage"], 1),
+             "max_abs_div": abs(a["cfl"]["flux_max"]), "cfl": a["cfl"]}
+        if name != "fp64":
+            for nm in ("u", "v", "w", "p"):
+                d[f"rel_l2_{nm}"] = float(np.linalg.norm(a["fields"][nm] - b["fields"][nm]) /
+                                          np.linalg.norm(b["fields"][nm]))
+            d["max_abs_div_diff_vs_fp64"] = abs(abs(a["cfl"]["flux_max"]) - abs(b["cfl"]["flux_max"]))
+        out[name] = d
+    out["clocks"] = clk
     print(json.dumps(out), flush=True)
     return 0
 
@@ -585,7 +608,7 @@ def run_adjoint_bench(args):
     nx, ny, layers, dt = WORKLOADS[args.workload]
     prisms = 2 * nx * ny * layers
     mesh = ng.make_mesh(nx, ny)
-    mixed = args.precision == "mixed"
+    mixed = args.precision in ("mixed", "mixed_f32")
     prm = ng.channel_params(nx, ny, layers, dt, precision=(ng.MIXED if mixed else ng.FP64))
     s = ng.Solver(prm, mesh)
     u0, v0, w0, p0 = ng.initial_channel(prm, s.ncell, seed=1)
@@ -749,11 +772,17 @@ def main():
                     help="host threads of the --impl reference arm (0: all cores)")
     ap.add_argument("--fp64-peak", action="store_true",
                     help="instead of timing the step: the device's FP64 FMA rate with clocks sampled")
-    ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"])
+    ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "mixed_f32", "both"])
+    ap.add_argument("--fp64-spmv", default="stored", choices=["stored", "matrix-free"],
+                    help="couplings of the FP64 arm's BiCGSTAB products")
+    ap.add_argument("--mixed-form", default="mixed", choices=["mixed", "mixed_f32"],
+                    help="the mixed-precision arm of --precision both (the headline value)")
     ap.add_argument("--profile-run", action="store_true",
                     help="device-timed region only (no end-to-end leg, no CPU baseline), for ncu captures")
     ap.add_argument("--accuracy-steps", type=int, default=0,
                     help="instead of timing: run both precisions N RK3 steps and print mixed-vs-FP64 errors")
+    ap.add_argument("--accuracy-compat0", action="store_true",
+                    help="with --accuracy-steps: also run the mixed form with the reference's quirks corrected")
     ap.add_argument("--adjoint-steps", type=int, default=0,
                     help="instead of timing the forward: adjoint/forward cost over N FP64 RK3 steps")
     ap.add_argument("--ckpt", type=int, default=20, help="checkpoint spacing of --adjoint-steps")

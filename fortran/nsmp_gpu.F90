@@ -17,7 +17,7 @@ module nsmp_gpu
   implicit none
 
   integer(c_int), parameter :: NSMP_OK = 0, NSMP_WARN_MAXITER = 1, NSMP_WARN_BREAKDOWN = 2
-  integer(c_int), parameter :: NSMP_FP64 = 0, NSMP_MIXED = 1
+  integer(c_int), parameter :: NSMP_FP64 = 0, NSMP_MIXED = 1, NSMP_MIXED_F32 = 2
   integer(c_int), parameter :: NSMP_F_U = 0, NSMP_F_V = 1, NSMP_F_W = 2, NSMP_F_P = 3,     &
        NSMP_F_U1FACE = 4, NSMP_F_U2FACE = 5, NSMP_F_U3FACE = 6, NSMP_F_UTFACE = 7,         &
        NSMP_F_UBFACE = 8, NSMP_F_RHSU = 9, NSMP_F_RHSV = 10, NSMP_F_RHSW = 11,             &
@@ -173,6 +173,11 @@ module nsmp_gpu
        import :: c_int, c_ptr
        type(c_ptr), value :: ctx
        integer(c_int), value :: mode
+     end function
+     integer(c_int) function nsmp_set_fp64_spmv(ctx, matrix_free) bind(C, name="nsmp_set_fp64_spmv")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: matrix_free
      end function
      integer(c_int) function nsmp_set_inner_solver(ctx, inner_tol, inner_cap, restart_every)   &
           bind(C, name="nsmp_set_inner_solver")

@@ -38,6 +38,9 @@ extern "C" {
 
 #define NSMP_FP64 0              /* plain form: FP64 throughout                         */
 #define NSMP_MIXED 1             /* FP32 stencils/Krylov + FP64 iterative refinement    */
+#define NSMP_MIXED_F32 2         /* NSMP_MIXED + the stage right-hand side (fluxes,
+                                    gradients, Smagorinsky, diffusion) in FP32; the
+                                    state, predictor update and AB2 history stay FP64 */
 
 /* Runtime parameters: dataParameters.txt (input_parameters.F90:240-442) and
  * the compile-time constants of common.mpf:59-113 that the path reads. */
@@ -57,7 +60,7 @@ typedef struct nsmp_params {
     int les;           /* 1: Smagorinsky (KeyLES, Iturbu = 1)                   */
     int les_van;       /* 1: van Driest damping (KeyLESVan), 0: Mason           */
     int ref_bug_compat;/* 1: reproduce the reference's arithmetic quirks        */
-    int precision;     /* NSMP_FP64 or NSMP_MIXED                               */
+    int precision;     /* NSMP_FP64, NSMP_MIXED or NSMP_MIXED_F32               */
     int device;        /* CUDA device ordinal                                   */
 } nsmp_params;
 
@@ -198,6 +201,12 @@ int nsmp_mass_diag_noalloc(nsmp_ctx* ctx, double out[4]);
  * test (eps) is unaffected: these trade hand-overs against iterations, not
  * accuracy.  The mixed mode needs an even number of interior layers. */
 int nsmp_set_inner_solver(nsmp_ctx* ctx, double inner_tol, int inner_cap, int restart_every);
+/* NSMP_FP64 pressure solver: 0 (default) applies A D^-1 with the Jacobi-
+ * scaled couplings stored once per prism (five FP64 arrays read by each
+ * product); 1 regenerates them matrix-free from the column and layer factors
+ * and D^-1 (five fewer arrays, ten more FP64 multiplies a prism).  The two
+ * give the same bits. */
+int nsmp_set_fp64_spmv(nsmp_ctx* ctx, int matrix_free);
 /* Stream used by the context (cudaStream_t as void*). */
 void* nsmp_stream(nsmp_ctx* ctx);
 

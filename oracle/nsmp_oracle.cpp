@@ -98,10 +98,17 @@ struct orc_ctx {
     R2 eddy, walld;
     int sg_init = 1;
     int flag_ab = 0;
+    int sum_reverse = 0;  // 1: add per-layer partial sums in reverse layer order
     orc_info info{};
 };
 
 namespace {
+
+// Order in which per-layer partial sums are added: layer order (the
+// default), or reversed -- a different but equally valid summation order,
+// used only to measure how sensitive the solver's iteration count is to the
+// rounding of its global sums.
+int g_sum_reverse = 0;
 
 // Per-layer partial sums added in layer order: deterministic for any
 // thread count.
@@ -111,7 +118,10 @@ double ksum(int k0, int k1, F f) {
 #pragma omp parallel for schedule(static)
     for (int k = k0; k <= k1; ++k) part[k - k0] = f(k);
     double s = 0.0;
-    for (double x : part) s += x;
+    if (g_sum_reverse)
+        for (auto it = part.rbegin(); it != part.rend(); ++it) s += *it;
+    else
+        for (double x : part) s += x;
     return s;
 }
 
@@ -1087,7 +1097,10 @@ void BICGSTAB_SOLVE(orc_ctx& c, R2& rhs, R2& phi) {
             q1[k] = s1; q2[k] = s2;
         }
         double sr1 = 0, sr2 = 0;
-        for (int k = 2; k <= NZ - 1; ++k) { sr1 += q1[k]; sr2 += q2[k]; }
+        for (int kk = 2; kk <= NZ - 1; ++kk) {
+            const int k = g_sum_reverse ? NZ + 1 - kk : kk;
+            sr1 += q1[k]; sr2 += q2[k];
+        }
         r2norm = std::sqrt(sr2);
         r1norm = sr1;
         e2norm = r2norm / b2norm;
@@ -1229,10 +1242,9 @@ R2* field_ptr(orc_ctx& c, int f) {
 }
 
 void set_threads(const orc_ctx& c) {
+    g_sum_reverse = c.sum_reverse;
 #ifdef _OPENMP
     if (c.P.nthreads > 0) omp_set_num_threads(c.P.nthreads);
-#else
-    (void)c;
 #endif
 }
 
@@ -1342,6 +1354,7 @@ int orc_set(orc_ctx* c, int field, const double* in) {
 }
 
 int orc_get_flag_ab(const orc_ctx* c) { return c->flag_ab; }
+void orc_set_sum_order(orc_ctx* c, int reverse) { c->sum_reverse = reverse ? 1 : 0; }
 void orc_set_flag_ab(orc_ctx* c, int f) { c->flag_ab = f; }
 
 int orc_step(orc_ctx* c, int fin_rk, orc_info* info) {

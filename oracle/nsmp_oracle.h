@@ -94,6 +94,10 @@ int orc_user_initial(orc_ctx* c, const double* u, const double* v,
 int orc_get(const orc_ctx* c, int field, double* out);
 int orc_set(orc_ctx* c, int field, const double* in);
 int orc_get_flag_ab(const orc_ctx* c);
+/* 1: add the per-layer partial sums of every global sum in reverse layer
+ * order (an equally valid order; for measuring the sensitivity of BiCGSTAB's
+ * iteration count to the rounding of its dot products), 0: layer order. */
+void orc_set_sum_order(orc_ctx* c, int reverse);
 void orc_set_flag_ab(orc_ctx* c, int f);
 
 /* One full time step (nsmp3D.F90:394-564): fin_rk 1 = Euler->AB2,

@@ -65,6 +65,7 @@ def lib():
             getattr(L, name).argtypes = [C.c_void_p]
             getattr(L, name).restype = C.c_int
         L.orc_set_flag_ab.argtypes = [C.c_void_p, C.c_int]
+        L.orc_set_sum_order.argtypes = [C.c_void_p, C.c_int]
         L.orc_ghost_image.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_no_cp.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_geom.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
@@ -197,6 +198,10 @@ class Oracle:
     @flag_ab.setter
     def flag_ab(self, f):
         lib().orc_set_flag_ab(self.h, int(f))
+
+    def set_sum_order(self, reverse):
+        """Reverse (True) or layer order (False) of the per-layer partial sums."""
+        lib().orc_set_sum_order(self.h, 1 if reverse else 0)
 
     def stats_reset(self):
         lib().orc_stats_reset(self.h)

@@ -222,13 +222,17 @@ def test_autograd_function_matches_the_adjoint():
 def test_adjoint_config3_against_finite_differences():
     """The 1,048,576-prism mesh (128x64 quads, 64 tanh layers, dt 5e-4,
     force 0.01 N(0,1), seed 2): the adjoint gradient over 10 RK3 steps with
-    a checkpoint every 5 against central differences with step 1e-6 along 8
-    seeded directions (PPE solves to 1e-13)."""
+    a checkpoint every 5 against central differences along 8 seeded
+    directions (PPE solves to 1e-13).  The step is 1e-3: J is about 0.2 and
+    its directional derivatives 1e-6 to 2e-5, so with a step of 1e-6 the
+    difference J+ - J- is only ~1e5 units of J's last place, and FP64
+    rounding of the forward run limits the agreement to 2e-6..1.5e-4
+    (measured); steps 1e-3 and 1e-4 give 2e-8..2e-6."""
     prm, mesh, s = _solver(128, 64, 64, 5e-4, eps=1e-13, max_iters=5000)
     n0, nz = prm["n0"], prm["nz"]
     fx = _interior_random(np.random.default_rng(2), n0, nz, 0.01)
     st = _state(s)
-    nsteps, h = 10, 1e-6
+    nsteps, h = 10, 1e-3
     s.upload_state(*st[0], st[1], st[2], 0)
     J, grad, rc = s.adjoint(nsteps, 5, fx)
     assert rc == 0

