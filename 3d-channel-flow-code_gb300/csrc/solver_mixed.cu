@@ -147,22 +147,6 @@ __device__ __forceinline__ void stv(float* p, size_t i, const FV<L>& o) {
     else *reinterpret_cast<float2*>(p + i) = make_float2(o.v[0], o.v[1]);
 }
 
-// L2 prefetch of the next grid-stride round.  Each warp's groups are L*32
-// consecutive values of every column vector; lane 0 asks the L2 for the
-// next round's range of a vector with one bulk prefetch (a hint: nothing
-// waits on it, and no register holds the data), so those loads find the L2
-// warm instead of waiting on DRAM.  The range is clipped to the vector's
-// end and to whole 16-byte units.
-template <int L>
-__device__ __forceinline__ void prefetch_round(const float* v, int hw_next, int ngrp) {
-    if (hw_next >= ngrp) return;
-    const int cnt = min(32, ngrp - hw_next);
-    const unsigned bytes = (unsigned)(L * cnt * (int)sizeof(float)) & ~15u;
-    if (bytes == 0) return;
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(v + (size_t)L * hw_next), "r"(bytes)
-                 : "memory");
-}
-
 // One BiCGSTAB iteration is two passes.  The p/v pass of iteration i carries
 // the tail of iteration i-1 (r = s - omega t and the correction increment
 // e += D^-1 (alpha p + omega s)) and forms the norms of that r; the s/t pass
@@ -222,21 +206,7 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
     // is issued before the shuffle and before any store of the group, so all
     // are in flight together; lanes past the end repeat the warp's first
     // group and store nothing.
-    const int stride = gridDim.x * blockDim.x;
-    for (int hw = blockIdx.x * blockDim.x + (threadIdx.x & ~31); hw < ngrp; hw += stride) {
-        if (lane == 0) {  // the own-column vectors of the next round (D^-1 and r^0 sit in the L2 window)
-            if (MODE == 2) {
-                prefetch_round<L>(a.s, hw + stride, ngrp);
-                prefetch_round<L>(a.t, hw + stride, ngrp);
-                prefetch_round<L>(a.e, hw + stride, ngrp);
-            } else {
-                prefetch_round<L>(a.r, hw + stride, ngrp);
-            }
-            if (MODE != 0) {
-                prefetch_round<L>(pin, hw + stride, ngrp);
-                prefetch_round<L>(vin, hw + stride, ngrp);
-            }
-        }
+    for (int hw = blockIdx.x * blockDim.x + (threadIdx.x & ~31); hw < ngrp; hw += gridDim.x * blockDim.x) {
         const int h = hw + lane;
         const bool act = h < ngrp;
         const int g = L * (act ? h : hw);
@@ -372,12 +342,7 @@ __global__ void __launch_bounds__(kBlock) k_in_st(Mesh m, MixArgs a, RedScratch 
     };
     auto z1 = [&](size_t i) { return fmaf(-al, v[i], a.r[i]); };
     const int lane = threadIdx.x & 31;
-    const int stride = gridDim.x * blockDim.x;
-    for (int hw = blockIdx.x * blockDim.x + (threadIdx.x & ~31); hw < ngrp; hw += stride) {
-        if (lane == 0) {  // the next round's r and v (D^-1 and r^0 sit in the L2 window)
-            prefetch_round<L>(a.r, hw + stride, ngrp);
-            prefetch_round<L>(v, hw + stride, ngrp);
-        }
+    for (int hw = blockIdx.x * blockDim.x + (threadIdx.x & ~31); hw < ngrp; hw += gridDim.x * blockDim.x) {
         const int h = hw + lane;
         const bool act = h < ngrp;
         const int g = L * (act ? h : hw);

@@ -166,14 +166,17 @@ def test_config0_rk3_at_reference_tolerance():
 
 
 @pytest.mark.slow
-@pytest.mark.parametrize("eps,tol,tol_p", [(1e-14, 1e-11, 3e-11), (1e-10, 1e-9, 1e-8)])
+@pytest.mark.parametrize("eps,tol,tol_p", [(1e-14, 1e-11, 3e-11), (1e-10, 5e-9, 5e-7)])
 def test_config1_one_step(eps, tol, tol_p):
     """The 1,048,576-prism case (128x64 quads, 64 tanh layers, dt 5e-4): one
-    RK3 step against the oracle, every field.  At eps = 1e-14, u, v, w agree
-    to 1e-11 and p to 3e-11 (measured 1.8e-11: the solver's relative
-    residual bounds p's error only to its conditioning); at eps = 1e-10 the
-    iterations stay within the oracle's summation-order spread (measured:
-    GPU 611/577/555, oracle 620/553/550)."""
+    RK3 step against the oracle, every field.  At eps = 1e-14, u, v, w and
+    the face fluxes agree to 1e-11 and p to 3e-11 (measured 1.8e-11: the
+    relative residual bounds p's error only up to the operator's
+    conditioning).  At eps = 1e-10 two solves that each meet the tolerance
+    differ by that tolerance times the conditioning: measured v 1.1e-9,
+    faces 2.6e-9, p 1.3e-7; the iterations stay within the oracle's
+    summation-order spread (measured: GPU 611/577/555, oracle
+    620/553/550)."""
     prm, mesh = small_case(128, 64, layers=64, dt=5e-4, eps=eps, max_iters=5000)
     o, s = _pair(prm, mesh)
     _, io = o.step(3)
