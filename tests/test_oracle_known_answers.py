@@ -108,7 +108,7 @@ def test_predictor_keeps_a_uniform_flow():
 
 def test_taylor_green_predictor_converges_to_funustar():
     """First-order convergence of the predictor's right-hand side to the
-    analytic funustar/funvstar (measured ratios 1.85, 1.96, 1.99)."""
+    analytic funustar/funvstar (measured ratios 1.85 and 1.96)."""
     errs = [predictor_error(n) for n in (8, 16, 32)]
     for (eu0, ev0), (eu1, ev1) in zip(errs, errs[1:]):
         assert eu0 / eu1 >= 1.7 and ev0 / ev1 >= 1.7, errs
