@@ -41,7 +41,8 @@ int nsmp_create(const nsmp_params* prm, const nsmp_mesh* mesh, nsmp_ctx** out) {
         // current device is given back when nsmp_create returns
         nsmp::DeviceGuard guard(c->device);
         std::string err;
-        int rc = nsmp::build_layout(*prm, *mesh, c->L, err);
+        // the floating-point geometry on the context's device, the topology on the host
+        int rc = nsmp::build_layout_device(*prm, *mesh, c->L, err);
         if (rc != 0) {
             delete c;
             return rc;
@@ -340,13 +341,23 @@ int nsmp_solver_counters(nsmp_ctx* c, long long* bicg_iters, long long* fp64_upd
     return NSMP_OK;
 }
 
-// Host-only diagnostic: geometry exactly as the setup computes it.
-int nsmp_geometry(const nsmp_params* prm, const nsmp_mesh* mesh, int which, double* out, int* count) {
+namespace {
+
+// Geometry array `which` as the host setup (device = -1) or the device setup
+// on ordinal `device` computes it.
+int geometry_of(const nsmp_params* prm, const nsmp_mesh* mesh, int which, double* out, int* count, int device) {
     if (!prm || !mesh || !out || !count) return NSMP_ERR_ARG;
     try {
         HostLayout L;
         std::string err;
-        int rc = nsmp::build_layout(*prm, *mesh, L, err);
+        int rc;
+        if (device >= 0) {
+            nsmp::DeviceGuard guard(device);
+            if (guard.err != cudaSuccess) return NSMP_ERR_CUDA;
+            rc = nsmp::build_layout_device(*prm, *mesh, L, err);
+        } else {
+            rc = nsmp::build_layout(*prm, *mesh, L, err);
+        }
         if (rc) return rc;
         const std::vector<double>* src = nullptr;
         switch (which) {
@@ -388,6 +399,18 @@ int nsmp_geometry(const nsmp_params* prm, const nsmp_mesh* mesh, int which, doub
     } catch (...) {
         return NSMP_ERR_NOMEM;
     }
+}
+
+}  // namespace
+
+// Host-only diagnostic: geometry exactly as the host setup computes it.
+int nsmp_geometry(const nsmp_params* prm, const nsmp_mesh* mesh, int which, double* out, int* count) {
+    return geometry_of(prm, mesh, which, out, count, -1);
+}
+
+int nsmp_geometry_device(const nsmp_params* prm, const nsmp_mesh* mesh, int which, double* out, int* count) {
+    if (!prm) return NSMP_ERR_ARG;
+    return geometry_of(prm, mesh, which, out, count, prm->device);
 }
 
 }  // extern "C"

@@ -113,5 +113,8 @@ struct HostLayout {
 // Builds the geometry and the device tables; returns 0 or an NSMP_ERR code
 // with a message in err.
 int build_layout(const nsmp_params& p, const nsmp_mesh& m, HostLayout& out, std::string& err);
+// The same tables, with the floating-point geometry computed on the current
+// device (bit-identical to build_layout; needs a GPU).
+int build_layout_device(const nsmp_params& p, const nsmp_mesh& m, HostLayout& out, std::string& err);
 
 }  // namespace nsmp

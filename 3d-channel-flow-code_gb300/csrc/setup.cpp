@@ -19,32 +19,14 @@
 
 #include "host_common.h"
 #include "layout.h"
+#include "setup_geo.h"
 
 namespace nsmp {
+namespace setup {
 namespace {
 
 const double kTolF = (double)1.0E-7f;  // default-REAL literal 1.0E-7 of the reference
 const double kTolD = 1.0e-7;           // 1.0d-7
-
-struct Geo {
-    int N0, NV, NZ, NC;
-    // mesh (0-based copies)
-    std::vector<int> vp;   // (N0,3): vertex (0-based)
-    std::vector<int> cp;   // (NCmax,3): neighbour (0-based, -1 = none)
-    std::vector<int> nbe, nbev;
-    std::vector<double> xv, yv;
-    // geometry
-    std::vector<double> xc, yc, area;                 // (NC)
-    std::vector<double> dxVV, dyVV, dlVV, xnn, ynn;   // (N0,3)
-    std::vector<double> dxCC, dyCC, dlCC, dle1, dle2, doe;
-    std::vector<double> sxx, syy, sxy;
-    std::vector<int> img;                             // ghost -> image cell (0-based)
-    std::vector<std::vector<std::pair<int, double>>> stencil;  // per vertex: (cell, weight)
-    std::vector<double> dlVsum;
-    std::vector<int> vpair, vedge;
-    double total_volume = 0.0;
-    int at(int i, int j) const { return i + j * N0; }
-};
 
 // Quantised coordinate key with a +-1 neighbourhood lookup, verified with the
 // reference's tolerance; equivalent to scanning every boundary vertex.
@@ -64,9 +46,12 @@ struct CoordIndex {
     }
 };
 
-int geometry(const nsmp_params& p, Geo& g, std::string& err) {
-    const int N0 = g.N0, NV = g.NV;
-    // cell centres, areas, edges, normals: calcul_geometry.F90:292-367
+}  // namespace
+
+// Cell centres, areas, edges, normals: calcul_geometry.F90:292-367.  The
+// centre and area arrays leave room for one ghost cell per boundary edge.
+void cell_geometry(Geo& g) {
+    const int N0 = g.N0;
     int nghost = 0;
     for (int i = 0; i < N0; ++i)
         for (int j = 0; j < 3; ++j)
@@ -98,7 +83,17 @@ int geometry(const nsmp_params& p, Geo& g, std::string& err) {
         vol = vol + g.area[i];
     }
     g.total_volume = vol;
+}
 
+// Ghost cells with their periodic images (calcul_geometry.F90:402-578) and
+// the periodic vertex pairs and corners (:893-1040).
+int ghosts_and_pairs(const nsmp_params& p, Geo& g, std::string& err) {
+    const int N0 = g.N0, NV = g.NV;
+    int nghost = 0;
+    for (int i = 0; i < N0; ++i)
+        for (int j = 0; j < 3; ++j)
+            if (g.cp[g.at(i, j)] < 0) ++nghost;
+    const int NCmax = N0 + nghost;
     // boundary vertex coordinate index and boundary edge -> cell map
     CoordIndex bidx;
     for (int nv = 0; nv < NV; ++nv)
@@ -205,8 +200,25 @@ int geometry(const nsmp_params& p, Geo& g, std::string& err) {
         g.vpair[nv] = pr;
     }
     if (ncorner != 4) { err = "expected 4 corner vertices"; return NSMP_ERR_MESH; }
+    return 0;
+}
 
-    // vertex stencils (surrounding/weight/dlVsum): calcul_geometry.F90:1055-1076
+// The cells around each vertex in the reference's visiting order (cell, then
+// corner): CSR over vertices of 3 * cell + corner.
+void vertex_incidence(const Geo& g, std::vector<int>& ptr, std::vector<int>& inc) {
+    ptr.assign(g.NV + 1, 0);
+    for (int i = 0; i < g.N0; ++i)
+        for (int j = 0; j < 3; ++j) ptr[g.vp[g.at(i, j)] + 1] += 1;
+    for (int v = 0; v < g.NV; ++v) ptr[v + 1] += ptr[v];
+    inc.assign(3 * (size_t)g.N0, 0);
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (int i = 0; i < g.N0; ++i)
+        for (int j = 0; j < 3; ++j) inc[fill[g.vp[g.at(i, j)]]++] = 3 * i + j;
+}
+
+// Vertex stencils (surrounding/weight/dlVsum): calcul_geometry.F90:1055-1076.
+void vertex_weights(Geo& g) {
+    const int N0 = g.N0, NV = g.NV;
     g.stencil.assign(NV, {});
     g.dlVsum.assign(NV, 0.0);
     for (int i = 0; i < N0; ++i)
@@ -217,8 +229,14 @@ int geometry(const nsmp_params& p, Geo& g, std::string& err) {
             g.stencil[nv].push_back({i, w});
             g.dlVsum[nv] = g.dlVsum[nv] + w;
         }
+}
 
-    // edge midpoints, centre-line intersections, doe: calcul_geometry.F90:1343-1387
+// Edge midpoints, centre-line intersections, doe (calcul_geometry.F90:1343-1387);
+// LSQ sums and Kim-Choi factors (:1460-1517).
+void edge_geometry(Geo& g) {
+    const int N0 = g.N0;
+    const size_t NCmax = g.cp.size() / 3;
+    auto CP = [&](int i, int j) { return g.cp[i + (size_t)j * NCmax]; };
     g.doe.assign(3 * N0, 0.0);
     for (int i = 0; i < N0; ++i)
         for (int j = 0; j < 3; ++j) {
@@ -259,8 +277,9 @@ int geometry(const nsmp_params& p, Geo& g, std::string& err) {
         }
         g.sxx[i] = sX; g.syy[i] = sY; g.sxy[i] = sXY;
     }
-    return 0;
 }
+
+namespace {
 
 // Reverse Cuthill-McKee over the periodic triangle adjacency; ties broken by
 // (degree, original number) so the permutation is deterministic.
@@ -300,7 +319,7 @@ std::vector<int> rcm(int N0, const std::vector<std::array<int, 3>>& adj) {
 
 }  // namespace
 
-int build_layout(const nsmp_params& p, const nsmp_mesh& m, HostLayout& L, std::string& err) {
+int read_mesh(const nsmp_params& p, const nsmp_mesh& m, Geo& g, std::string& err) {
     if (p.n0 <= 0 || p.nvert <= 0 || p.nz < 4) { err = "bad sizes"; return NSMP_ERR_ARG; }
     if (!(p.xdfin > p.xdini) || !(p.ydfin > p.ydini) || !(p.sigfin > p.sigini)) { err = "bad box"; return NSMP_ERR_ARG; }
     if (p.top_bc < 0 || p.top_bc > 1 || p.bot_bc < 0 || p.bot_bc > 1) {
@@ -308,7 +327,6 @@ int build_layout(const nsmp_params& p, const nsmp_mesh& m, HostLayout& L, std::s
         return NSMP_ERR_UNSUPPORTED;
     }
     if (!(p.dt > 0.0) || !(p.re > 0.0) || !(p.eps > 0.0) || p.max_iters < 0) { err = "bad dt/Re/eps/MaxIters"; return NSMP_ERR_ARG; }
-    Geo g;
     g.N0 = p.n0; g.NV = p.nvert; g.NZ = p.nz;
     g.vp.resize(3 * (size_t)g.N0); g.cp.resize(3 * (size_t)g.N0);
     g.nbe.assign(m.nbe, m.nbe + g.N0); g.nbev.assign(m.nbev, m.nbev + g.NV);
@@ -321,8 +339,13 @@ int build_layout(const nsmp_params& p, const nsmp_mesh& m, HostLayout& L, std::s
         g.vp[q] = m.No_vp[q] - 1;
         g.cp[q] = m.No_cp[q] - 1;
     }
-    int rc = geometry(p, g, err);
-    if (rc) return rc;
+    return 0;
+}
+
+// Adjacency, renumbering, vertex classes and stencils, the sigma grid and
+// level factors, and the device tables in the new column order, from the
+// finished geometry.
+int finish_layout(const nsmp_params& p, Geo& g, HostLayout& L, std::string& err) {
     const int N0 = g.N0, NV = g.NV, NZ = g.NZ, NC = g.NC;
     const size_t NCmax = g.cp.size() / 3;
     auto CP = [&](int i, int j) { return g.cp[i + (size_t)j * NCmax]; };
@@ -496,6 +519,32 @@ int build_layout(const nsmp_params& p, const nsmp_mesh& m, HostLayout& L, std::s
         for (int j = 0; j < 3; ++j) L.ref_No_cp[i + (size_t)j * NC] = CP(i, j) + 1;
     for (int gh = N0; gh < NC; ++gh) L.ref_No_cp[gh + 2 * (size_t)NC] = g.img[gh - N0] + 1;
     return 0;
+}
+
+}  // namespace setup
+
+// The whole setup on the host: the reference's arithmetic step by step.
+int build_layout(const nsmp_params& p, const nsmp_mesh& m, HostLayout& L, std::string& err) {
+    setup::Geo g;
+    int rc = setup::read_mesh(p, m, g, err);
+    if (rc) return rc;
+    setup::cell_geometry(g);
+    rc = setup::ghosts_and_pairs(p, g, err);
+    if (rc) return rc;
+    setup::vertex_weights(g);
+    setup::edge_geometry(g);
+    return setup::finish_layout(p, g, L, err);
+}
+
+// The same setup with its floating-point steps on the current device: the
+// same bits (setup_gpu.cu), the topology and table packing on the host.
+int build_layout_device(const nsmp_params& p, const nsmp_mesh& m, HostLayout& L, std::string& err) {
+    setup::Geo g;
+    int rc = setup::read_mesh(p, m, g, err);
+    if (rc) return rc;
+    rc = setup::device_steps(p, g, err);
+    if (rc) return rc;
+    return setup::finish_layout(p, g, L, err);
 }
 
 }  // namespace nsmp

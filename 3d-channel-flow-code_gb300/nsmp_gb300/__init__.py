@@ -66,7 +66,7 @@ EXPORTS = [
     "nsmp_set_body_force", "nsmp_wall_shear", "nsmp_adjoint", "nsmp_apply_A", "nsmp_apply_AT",
     "nsmp_set_adjoint_budget", "nsmp_stats_reset", "nsmp_stats_sample", "nsmp_stats_count",
     "nsmp_stats_download", "nsmp_stats_plane", "nsmp_download_vertex", "nsmp_cfl_diag",
-    "nsmp_solver_counters", "nsmp_probe_fp64_fma", "nsmp_set_fp64_spmv",
+    "nsmp_solver_counters", "nsmp_probe_fp64_fma", "nsmp_set_fp64_spmv", "nsmp_geometry_device",
 ]
 
 # glob_cfl values of nsmp_cfl_diag (NSMP_CFL_* order)
@@ -141,6 +141,7 @@ def lib(build_if_missing=True):
     L.nsmp_initial_channel.argtypes = [P(Params), C.c_int, C.c_double, C.c_double, C.c_ulonglong] + [vp] * 4
     L.nsmp_sigma_grid.argtypes = [P(Params)] + [vp] * 4
     L.nsmp_geometry.argtypes = [P(Params), P(Mesh), C.c_int, vp, P(C.c_int)]
+    L.nsmp_geometry_device.argtypes = [P(Params), P(Mesh), C.c_int, vp, P(C.c_int)]
     L.nsmp_prof_enable.argtypes = [vp, C.c_int]
     L.nsmp_prof_read.argtypes = [vp, C.c_int, P(C.c_longlong), P(C.c_double)]
     L.nsmp_counters.argtypes = [vp, P(C.c_longlong), P(C.c_longlong)]
@@ -202,14 +203,16 @@ def n_cell_of(mesh):
     return int(mesh["No_cp"].shape[0] + np.count_nonzero(np.asarray(mesh["No_cp"]) == 0))
 
 
-def geometry(params, mesh, which):
-    """Geometry array as computed by the library's setup (host only)."""
+def geometry(params, mesh, which, device=False):
+    """Geometry array as computed by the library's host setup, or (device=True)
+    by the setup nsmp_create runs, with its floating-point steps on the GPU."""
     L = lib()
     ms, keep = mesh_struct(mesh)
     ncell = n_cell_of(mesh)
     out = np.zeros(max(3 * ncell, params["nvert"], params["nz"]), dtype=np.float64)
     cnt = C.c_int(0)
-    rc = L.nsmp_geometry(C.byref(to_struct(params)), C.byref(ms), which, _p(out), C.byref(cnt))
+    fn = L.nsmp_geometry_device if device else L.nsmp_geometry
+    rc = fn(C.byref(to_struct(params)), C.byref(ms), which, _p(out), C.byref(cnt))
     if rc:
         raise RuntimeError(f"nsmp_geometry failed ({rc})")
     return out[:cnt.value].copy()

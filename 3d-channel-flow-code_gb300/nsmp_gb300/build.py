@@ -52,10 +52,16 @@ def _stamp():
     return h.hexdigest()
 
 
+# Translation units whose floating-point results must equal the host
+# setup's bit for bit: no multiply-add contraction.
+NO_FMA = {"setup_gpu.cu"}
+
+
 def _compile(src, extra):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     if src.endswith(".cu"):
-        cmd = [NVCC] + NVFLAGS + extra + ["-c", src, "-o", obj]
+        own = ["-fmad=false"] if os.path.basename(src) in NO_FMA else []
+        cmd = [NVCC] + NVFLAGS + own + extra + ["-c", src, "-o", obj]
     else:
         cmd = ["g++"] + CXXFLAGS + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -760,6 +760,30 @@ def run_fp64_peak(args):
     return 0
 
 
+def run_setup(args):
+    """The setup of the workload's mesh: host path (nsmp_geometry) against
+    the path nsmp_create runs, with its floating-point geometry on the GPU
+    (nsmp_geometry_device), wall clock over several repetitions."""
+    import nsmp_gb300 as ng
+    nx, ny, layers, dt = WORKLOADS[args.workload]
+    mesh = ng.make_mesh(nx, ny)
+    prm = ng.channel_params(nx, ny, layers, dt)
+    ng.geometry(prm, mesh, ng.G_XC, device=True)  # first use: context creation, module load
+    clocks = ClockSampler(0)
+    clocks.start()
+    out = {"setup": "geometry + topology + device tables of the workload's mesh", "workload": workload_desc(args.workload)}
+    for name, dev in (("host_s", False), ("device_s", True)):
+        ts = []
+        for _ in range(max(3, args.steps)):
+            t0 = time.perf_counter()
+            ng.geometry(prm, mesh, ng.G_XC, device=dev)
+            ts.append(time.perf_counter() - t0)
+        out[name] = round(float(np.median(ts)), 4)
+    out["clocks"] = clocks.stop()
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -770,6 +794,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--ref-threads", type=int, default=0,
                     help="host threads of the --impl reference arm (0: all cores)")
+    ap.add_argument("--setup", action="store_true",
+                    help="instead of timing the step: the mesh setup, host path against device path")
     ap.add_argument("--fp64-peak", action="store_true",
                     help="instead of timing the step: the device's FP64 FMA rate with clocks sampled")
     ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "mixed_f32", "both"])
@@ -793,6 +819,8 @@ def main():
     args = ap.parse_args()
     if args.fp64_peak:
         return run_fp64_peak(args)
+    if args.setup:
+        return run_setup(args)
     if args.aux:
         return run_aux(args)
     if args.accuracy_steps > 0:

@@ -349,6 +349,13 @@ enum {
 };
 int nsmp_geometry(const nsmp_params* prm, const nsmp_mesh* mesh, int which,
                   double* out, int* count);
+/* The same arrays from the setup nsmp_create runs: the floating-point
+ * geometry (calcul_geometry's cell, edge and vertex-weight formulas) computed
+ * on device prm->device, the topology (ghosts, periodic images, vertex
+ * classes, renumbering) on the host.  Equal to nsmp_geometry bit for bit;
+ * needs a GPU. */
+int nsmp_geometry_device(const nsmp_params* prm, const nsmp_mesh* mesh, int which,
+                         double* out, int* count);
 
 #ifdef __cplusplus
 }
