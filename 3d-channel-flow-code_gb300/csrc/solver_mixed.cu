@@ -634,16 +634,13 @@ int mixed_alloc(nsmp_ctx* c) {
         return e;
     };
     for (double** p : {&c->b64, &c->xa, &c->xb}) CK(dalloc((void**)p, ncf * sizeof(double)));
-    for (float** p : {&c->r32, &c->p32[0], &c->p32[1], &c->v32[0], &c->v32[1], &c->s32, &c->t32})
+    for (float** p : {&c->r32, &c->p32[0], &c->p32[1], &c->v32[0], &c->v32[1], &c->s32, &c->t32, &c->e32})
         CK(dalloc((void**)p, ncf * sizeof(float)));
     // D^-1 and the shadow residual are read by both passes of every
-    // iteration and never written inside a Krylov process, and the
-    // correction e is read and written by every p/v pass: one block, so a
-    // single L2 access-policy window can keep them resident (all three when
-    // they fit the persisting set-aside, else D^-1 and r0)
-    CK(dalloc((void**)&c->invD32, 3 * ncf * sizeof(float)));
+    // iteration and never written inside a Krylov process: one block, so a
+    // single L2 access-policy window can keep them resident
+    CK(dalloc((void**)&c->invD32, 2 * ncf * sizeof(float)));
     c->r032 = c->invD32 + ncf;
-    c->e32 = c->invD32 + 2 * ncf;
     CK(dalloc((void**)&c->d_ppe32, sizeof(ColPPE32) * L.N0));
     const int nzp = (L.NZ - 2 + 3) / 4 * 4;  // interior layers, rounded up to a float4
     CK(dalloc((void**)&c->lev32, sizeof(float) * (3 * nzp + 4 * (size_t)L.NZ)));
@@ -783,24 +780,10 @@ struct L2Window {
     }
 };
 
-// Bytes of the block to keep L2-resident: D^-1, r0 and e when the three fit
-// the device's persisting set-aside and window, else D^-1 and r0.
-static size_t l2_window_bytes(nsmp_ctx* c) {
-    const size_t ncf = (size_t)c->mesh.N0 * c->mesh.NZ, np = (size_t)c->mesh.nprism;
-    const size_t three = (2 * ncf + np) * sizeof(float), two = (ncf + np) * sizeof(float);
-    int maxwin = 0, maxpers = 0;
-    if (cudaDeviceGetAttribute(&maxwin, cudaDevAttrMaxAccessPolicyWindowSize, c->device) != cudaSuccess ||
-        cudaDeviceGetAttribute(&maxpers, cudaDevAttrMaxPersistingL2CacheSize, c->device) != cudaSuccess) {
-        cudaGetLastError();
-        return two;
-    }
-    return (three <= (size_t)maxwin && three <= (size_t)maxpers) ? three : two;
-}
-
 int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     const Mesh& m = c->mesh;
     cudaStream_t st = c->stream;
-    L2Window l2win(c, l2_window_bytes(c));
+    L2Window l2win(c, (size_t)m.nprism * sizeof(float) + (size_t)m.N0 * m.NZ * sizeof(float));
     if (m.NZI & 1) {
         c->err = "mixed precision needs an even number of layers";
         return NSMP_ERR_UNSUPPORTED;
