@@ -102,7 +102,10 @@ enum {
 /* ---- setup: replaces nsmp3D.F90:232-249 device-side ------------------- */
 
 /* Builds the geometry (calcul_geometry, adjust_bc, PDE_center restated),
- * renumbers columns (reverse Cuthill-McKee) and uploads everything. */
+ * renumbers columns (reverse Cuthill-McKee) and uploads everything.  The
+ * floating-point geometry is computed on the context's device (the same bits
+ * as the host restatement of nsmp_geometry), the integer topology on the
+ * host. */
 int nsmp_create(const nsmp_params* prm, const nsmp_mesh* mesh, nsmp_ctx** out);
 int nsmp_destroy(nsmp_ctx* ctx);
 const char* nsmp_last_error(const nsmp_ctx* ctx);
