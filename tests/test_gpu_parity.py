@@ -388,3 +388,52 @@ def test_matrix_free_fp64_spmv_gives_the_same_bits():
         assert s.step(3, 1)[0] == 0
     for f in (ng.F_U, ng.F_V, ng.F_W, ng.F_P):
         assert np.array_equal(a.download(f), b.download(f))
+
+
+@pytest.mark.parametrize("variant", [dict(top_bc=1, bot_bc=1), dict(top_bc=1), dict(ref_bug_compat=0),
+                                     dict(les_van=0), dict(les=0, grid_kind=0, ref_bug_compat=0)])
+def test_one_step_variants(variant):
+    """The other supported paths through the stage, one RK3 step with both
+    solves converged to 1e-14: free-slip walls (BCvelcenter3D mirror signs,
+    BC.F90:459-527), the reference's quirks corrected, Mason instead of van
+    Driest damping (sgdamp, sgm_les.F90:1247-1281)."""
+    prm, mesh = small_case(10, 6, layers=8, eps=TIGHT, max_iters=3000, **variant)
+    o, s = _pair(prm, mesh)
+    o.step(3)
+    s.step(3, 1)
+    _compare(o, s, 1e-11, f"variant {variant}")
+
+
+def test_smallest_supported_mesh():
+    """3x3 quads (18 triangles) and two interior layers: the fewest the
+    periodic pairing and the vertical stencils allow."""
+    prm, mesh = small_case(3, 3, layers=2, eps=TIGHT, max_iters=500)
+    o, s = _pair(prm, mesh)
+    o.step(3)
+    s.step(3, 1)
+    _compare(o, s, 1e-11, "3x3x2")
+
+
+def test_mixed_precision_rejects_an_odd_layer_count():
+    """The FP32 passes pair layers: an odd interior layer count is refused
+    with NSMP_ERR_UNSUPPORTED and a message, and the FP64 form still runs."""
+    prm, mesh = small_case(8, 6, layers=7, precision=ng.MIXED)
+    s = ng.Solver(prm, mesh)
+    s.user_initial(*ng.initial_channel(prm, s.ncell, seed=1))
+    with pytest.raises(ng.NsmpError) as ei:
+        s.step(1, 1)
+    assert ei.value.code == ng.ERR_UNSUPPORTED and "even number of layers" in str(ei.value)
+    s.set_precision(ng.FP64)
+    assert s.step(1, 1)[0] == 0
+
+
+@pytest.mark.slow
+def test_config1_100_steps():
+    """configs[1]: the 1,048,576-prism case after 100 RK3 steps against the
+    oracle, every field, PPE solves to 1e-13 (spec: <= 1e-8)."""
+    prm, mesh = small_case(128, 64, layers=64, dt=5e-4, eps=1e-13, max_iters=5000)
+    o, s = _pair(prm, mesh)
+    for _ in range(100):
+        o.step(3)
+        assert s.step(3, 1)[0] == 0
+    _compare(o, s, 1e-8, "config1 100 steps")
