@@ -33,6 +33,8 @@
 //
 // An iteration is two stencil passes that fuse the vector updates (evaluated
 // at the seven stencil points) with the operator; it moves 17 FP32 vectors.
+// The p/v pass forms A D^-1 p from the two products already stored (see
+// pv_in1), which halves its lateral-neighbour loads.
 // Dot products are formed in FP32 per thread and warp and summed across
 // warps and blocks in FP64.
 #include <algorithm>
@@ -162,25 +164,34 @@ __device__ __forceinline__ void stv(float* p, size_t i, const FV<L>& o) {
 // while the operator's input D^-1 p is then p~ itself, so a stencil point
 // needs no D^-1 load.  D^-1 is read only at the centre, where v~ = D^-1 A p~
 // is formed and the unscaled values the dots need are recovered.
+//
+// In modes 0 and 1, v~ = M p~ (M = D^-1 A) is formed from p~ at the seven
+// stencil points.  In mode 2 the same product follows from the two stored
+// ones, M s~ = t~ (s/t pass) and M p~ = v~ (previous p/v pass), by linearity:
+//   M p~' = M (s~ - om t~ + beta (p~ - om v~)) = w - om M w,  w = t~ + beta v~,
+// so a lateral neighbour contributes two loads (t~, v~) instead of four
+// (s~, t~, p~, v~).  The recurrence carries the rounding of the earlier v~
+// forward; every FP64 update is followed by a mode-1 pass, which forms
+// M p~ directly again.
 template <int MODE>
-__device__ __forceinline__ float pv_p1(const MixArgs& a, const float* pin, const float* vin, float beta, float om,
-                                       size_t i) {  // p~ at one point
+__device__ __forceinline__ float pv_in1(const MixArgs& a, const float* pin, const float* vin, float beta, float om,
+                                        size_t i) {  // operator input at one point: p~ (modes 0, 1) or w (mode 2)
     if (MODE == 0) return a.r[i];
-    const float r = (MODE == 1) ? a.r[i] : fmaf(-om, a.t[i], a.s[i]);
-    return fmaf(beta, fmaf(-om, vin[i], pin[i]), r);
+    if (MODE == 2) return fmaf(beta, vin[i], a.t[i]);
+    return fmaf(beta, fmaf(-om, vin[i], pin[i]), a.r[i]);
 }
 
 template <int MODE, int L>
-__device__ __forceinline__ FV<L> pv_yv(const MixArgs& a, const float* pin, const float* vin, float beta, float om,
-                                       size_t i) {  // p~ = D^-1 p at layers i .. i+L-1
-    FV<L> r, y;
+__device__ __forceinline__ FV<L> pv_in(const MixArgs& a, const float* pin, const float* vin, float beta, float om,
+                                       size_t i) {  // the same at layers i .. i+L-1
+    FV<L> y;
     if (MODE == 2) {
-        const FV<L> ss = ldv<L>(a.s, i), tt = ldv<L>(a.t, i);
+        const FV<L> tt = ldv<L>(a.t, i), vv = ldv<L>(vin, i);
 #pragma unroll
-        for (int l = 0; l < L; ++l) r[l] = fmaf(-om, tt[l], ss[l]);
-    } else {
-        r = ldv<L>(a.r, i);
+        for (int l = 0; l < L; ++l) y[l] = fmaf(beta, vv[l], tt[l]);
+        return y;
     }
+    const FV<L> r = ldv<L>(a.r, i);
     if (MODE == 0) return r;
     const FV<L> pp = ldv<L>(pin, i), vv = ldv<L>(vin, i);
 #pragma unroll
@@ -215,9 +226,9 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
         const FV<L> dd = ldv<L>(a.invD, g), q0 = ldv<L>(a.r0, g);
         const bool ldT = act && kk + L < NZI && (lane == 31 || h + 1 >= ngrp);
         const bool ldB = act && kk > 0 && lane == 0;
-        const float eT = ldT ? pv_p1<MODE>(a, pin, vin, beta, om, g + L) : 0.f;
-        const float eB = ldB ? pv_p1<MODE>(a, pin, vin, beta, om, g - 1) : 0.f;
-        FV<L> r, p, e;
+        const float eT = ldT ? pv_in1<MODE>(a, pin, vin, beta, om, g + L) : 0.f;
+        const float eB = ldB ? pv_in1<MODE>(a, pin, vin, beta, om, g - 1) : 0.f;
+        FV<L> r, p, e, y;  // y: the operator input (p~, or w in mode 2)
         if (MODE == 2) {
             const FV<L> ss = ldv<L>(a.s, g), tt = ldv<L>(a.t, g), pp = ldv<L>(pin, g), vv = ldv<L>(vin, g);
             e = ldv<L>(a.e, g);
@@ -225,6 +236,7 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
             for (int l = 0; l < L; ++l) {
                 r[l] = fmaf(-om, tt[l], ss[l]);
                 p[l] = fmaf(beta, fmaf(-om, vv[l], pp[l]), r[l]);
+                y[l] = fmaf(beta, vv[l], tt[l]);
                 // increment of the previous iteration: e += D^-1 (alpha p + omega s)
                 e[l] = e[l] + fmaf(om, ss[l], al * pp[l]);
             }
@@ -236,12 +248,13 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
 #pragma unroll
                 for (int l = 0; l < L; ++l) p[l] = fmaf(beta, fmaf(-om, vv[l], pp[l]), r[l]);
             }
+            y = p;
         }
-        const FV<L> n1 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[0] - c) * NZI);
-        const FV<L> n2 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[1] - c) * NZI);
-        const FV<L> n3 = pv_yv<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[2] - c) * NZI);
-        float yT = __shfl_down_sync(0xffffffffu, p[0], 1);
-        float yB = __shfl_up_sync(0xffffffffu, p[L - 1], 1);
+        const FV<L> n1 = pv_in<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[0] - c) * NZI);
+        const FV<L> n2 = pv_in<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[1] - c) * NZI);
+        const FV<L> n3 = pv_in<MODE, L>(a, pin, vin, beta, om, g + (size_t)(P.nb[2] - c) * NZI);
+        float yT = __shfl_down_sync(0xffffffffu, y[0], 1);
+        float yB = __shfl_up_sync(0xffffffffu, y[L - 1], 1);
         if (!act) continue;
         if (kk + L >= NZI) yT = 0.f;
         else if (ldT) yT = eT;
@@ -251,8 +264,9 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
 #pragma unroll
         for (int l = 0; l < L; ++l) {
             const float4 q = __ldg(a.lev4 + kk + 1 + l);
-            v[l] = a_row32(P, q.x, q.y, q.z, p[l], n1[l], n2[l], n3[l], (l + 1 < L) ? p[l + 1] : yT,
-                           (l > 0) ? p[l - 1] : yB) * dd[l];  // v~ = D^-1 A p~
+            const float my = a_row32(P, q.x, q.y, q.z, y[l], n1[l], n2[l], n3[l], (l + 1 < L) ? y[l + 1] : yT,
+                                     (l > 0) ? y[l - 1] : yB) * dd[l];  // M y = D^-1 A y
+            v[l] = (MODE == 2) ? fmaf(-om, my, y[l]) : my;                // v~ = M p~
         }
         if (MODE == 2) {
 #pragma unroll
@@ -279,11 +293,11 @@ __device__ __forceinline__ void pv_cells(const Mesh& m, const MixArgs& a, int it
 // In mode 2 it also forms the norms of r and takes the hand-over test: when
 // it fires, alpha is left as it was, so that the pass repeated after the FP64
 // update (mode 1, same iteration index) continues the same Krylov process.
-// Capped at 64 registers (4 blocks of 256 per SM instead of 3): the pass is
-// latency-bound and the extra resident warps outweigh a few spilled values
-// (8 % faster at 6.3M prisms).
+// Three blocks of 256 per SM (80 registers): with the recurrence of mode 2 a
+// 64-register cap (four blocks) spills twice as much and runs 16 % slower
+// at 6.3M prisms.
 template <int L>
-__global__ void __launch_bounds__(kBlock, 4) k_in_pv(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
+__global__ void __launch_bounds__(kBlock, 3) k_in_pv(Mesh m, MixArgs a, RedScratch rs, Scal* sc) {
     pdl_enter();
     if (sc->done || sc->pending) return;
     const int it = sc->iiter;
