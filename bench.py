@@ -47,9 +47,15 @@ WORDS = {
     "k_bicg_init": 2 + 3, "k_bicg_p": 4, "k_bicg_spmv_v": 4, "k_bicg_s": 3, "k_bicg_spmv_t": 3,
     "k_bicg_x": 8, "k_pmean": 1, "k_vertex1": 1 + 0.5, "k_project": 1 + 0.5 + 3 + 5 + 4 + 5,
 }
-# FP64 flops per prism of the solver kernels (multiply, add and FMA counted as
-# 1, 1 and 2 flops; reciprocal of the Jacobi diagonal precomputed).
-FLOPS = {"k_bicg_spmv_v": 33, "k_bicg_spmv_t": 34, "k_bicg_x": 13, "k_bicg_p": 4, "k_bicg_s": 2}
+# FP64 flops per prism that the solver kernels execute (multiply, add and FMA
+# counted as 1, 1 and 2 flops), by form of the SpMV.  Stored couplings: five
+# FMAs a row plus the fused dots, (r0, v) or (t, s) and (t, t).  Matrix-free:
+# two more multiplies a coupling, kA_j dsigv and the neighbour's D^-1.
+# k_bicg_x: x += D^-1 (alpha p + omega s), r = s - omega t, |r|^2, |r|_1,
+# (r0, r); k_bicg_p: p = r + beta (p - omega v); k_bicg_s: s = r - alpha v.
+_FLOPS_VEC = {"k_bicg_x": 12, "k_bicg_p": 4, "k_bicg_s": 2}
+FLOPS = {"stored": dict(_FLOPS_VEC, k_bicg_spmv_v=12, k_bicg_spmv_t=14),
+         "matrix-free": dict(_FLOPS_VEC, k_bicg_spmv_v=22, k_bicg_spmv_t=24)}
 
 
 # bench precision names -> the library's precision modes
@@ -354,7 +360,22 @@ def step_bytes(prof, iters, updates, steps, prisms, mixed):
     return fixed + (per_iter * iters + per_upd * updates) / max(steps, 1), per_iter, per_upd, fixed
 
 
-def roofline(prof, iters, prisms, mixed, fp64_peak=None):
+def kernel_us(prof, iters, updates):
+    """Average device time of each kernel per launch that did work, in us:
+    per iteration for the iteration passes, per FP64 update for the
+    hand-over kernels, per launch for the rest.  The idle launches of the
+    solver loops (a few us each) are included in the totals."""
+    out = {}
+    for k, (n, ms) in prof.items():
+        if not n:
+            continue
+        real = iters if k in ITER_KERNELS else updates if k in UPDATE_KERNELS else n
+        if real:
+            out[k] = round(ms * 1e3 / real, 2)
+    return out
+
+
+def roofline(prof, iters, prisms, mixed, fp64_peak=None, spmv="stored"):
     hbm_peak, peak_kind = load_peaks()
     words = dict(WORDS)
     if mixed:
@@ -373,7 +394,7 @@ def roofline(prof, iters, prisms, mixed, fp64_peak=None):
             tr = json.load(fh).get("mixed" if mixed else "fp64", {})
         if dom in tr:
             traffic = tr[dom] * prisms
-    fl = None if mixed else FLOPS.get(dom)
+    fl = None if mixed else FLOPS[spmv].get(dom)
     total = sum(v[1] for v in prof.values())
     shares = {k: round(v[1] / max(total, 1e-12), 4) for k, v in prof.items() if v[0]}
     roof = {"bound": "hbm", "kernel": dom,
@@ -430,8 +451,9 @@ def run_ours(args):
         # per-kernel device times over K further steps of the same run
         rp = timed_region(s, ng, torch, stream, args.steps, pg, local, profile=True)
         r["prof"], r["prof_ms"], r["prof_iters"] = rp["prof"], rp["ms"], rp["iters"]
+        r["kernel_us"] = kernel_us(rp["prof"], rp["iters"], rp["updates"])
         r["roof"], r["shares"], r["busy_ms"] = roofline(rp["prof"], rp["iters"], prisms, prec != "fp64",
-                                                        fp64_peak)
+                                                        fp64_peak, spmv=args.fp64_spmv)
         # whole step: the timed region's iterations and FP64 updates with the
         # per-kernel bytes of the profiled region
         _, b_it, b_up, b_fix = step_bytes(rp["prof"], rp["iters"], rp["updates"], args.steps, prisms,
@@ -449,7 +471,7 @@ def run_ours(args):
     if args.profile_run:
         if rank == 0:
             print(json.dumps({"metric": "Mcell-steps/s", "value": r["value"], "profile_run": True,
-                              "precision": head, "kernel_share": r["shares"],
+                              "precision": head, "kernel_share": r["shares"], "kernel_us": r["kernel_us"],
                               "bicgstab_iters_per_stage": r["iters"] / (3.0 * args.steps)}), flush=True)
         for sv in solvers.values():
             sv[0].close()
@@ -517,6 +539,7 @@ def run_ours(args):
                        "bicgstab_iters_per_stage": round(r["iters"] / (3.0 * args.steps), 1)},
             "roofline": r["roof"],
             "kernel_share": r["shares"],
+            "kernel_us": r["kernel_us"],
             "device_busy_frac": round(r["busy_ms"] / max(r["prof_ms"], 1e-9), 4),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d,
@@ -531,7 +554,8 @@ def run_ours(args):
             f = res["fp64"]
             line["fp64"] = {"value": f["value"], "ms_per_step": f["ms_max"] / args.steps, "spmv": args.fp64_spmv,
                             "bicgstab_iters_per_stage": round(f["iters"] / (3.0 * args.steps), 1),
-                            "roofline": f["roof"], "kernel_share": f["shares"], "gpu_launches": f["launches"],
+                            "roofline": f["roof"], "kernel_share": f["shares"], "kernel_us": f["kernel_us"],
+                            "gpu_launches": f["launches"],
                             "clocks": f["clocks"]}
         if cmp:
             line["mixed_vs_fp64"] = cmp

@@ -31,14 +31,36 @@ def test_roofline_of_the_mixed_solver():
     assert roof["fp64_tflops"] is None  # FP32 kernel
 
 
+def test_kernel_times_are_per_launch_that_did_work():
+    # iteration passes per iteration, hand-over kernels per FP64 update,
+    # everything else per launch; kernels that never launched are left out
+    prof = {"k_in_pv": (1100, 67.0), "k_in_st": (1100, 40.0), "k_mix_scale": (140, 3.0),
+            "k_stage_rhs": (3, 7.2), "k_project": (0, 0.0)}
+    us = bench.kernel_us(prof, iters=1000, updates=30)
+    assert us == {"k_in_pv": 67.0, "k_in_st": 40.0, "k_mix_scale": 100.0, "k_stage_rhs": 2400.0}
+
+
 def test_roofline_of_the_fp64_solver_reports_its_fp64_rate():
     prisms, iters = 1048576, 500
     prof = {"k_bicg_x": (500, 17.5), "k_bicg_p": (500, 5.0)}
     roof, _, _ = bench.roofline(prof, iters, prisms, mixed=False)
     assert roof["kernel"] == "k_bicg_x"
     assert roof["algorithmic_bytes_per_launch"] == 8 * 8 * prisms
-    flops = bench.FLOPS["k_bicg_x"] * prisms * iters
+    flops = bench.FLOPS["stored"]["k_bicg_x"] * prisms * iters
     assert math.isclose(roof["fp64_tflops"], round(flops / 0.0175 / 1e12, 3))
+
+
+def test_fp64_spmv_flops_follow_the_form_that_runs():
+    # the stored-coupling SpMV executes five FMAs a row plus its dots; the
+    # matrix-free one two more multiplies a coupling (ten a row)
+    prisms, iters = 1048576, 500
+    prof = {"k_bicg_spmv_t": (500, 20.0)}
+    st, _, _ = bench.roofline(prof, iters, prisms, mixed=False, spmv="stored")
+    mf, _, _ = bench.roofline(prof, iters, prisms, mixed=False, spmv="matrix-free")
+    assert bench.FLOPS["stored"]["k_bicg_spmv_t"] == 5 * 2 + 2 * 2
+    assert bench.FLOPS["matrix-free"]["k_bicg_spmv_t"] - bench.FLOPS["stored"]["k_bicg_spmv_t"] == 10
+    assert math.isclose(st["fp64_tflops"], round(14 * prisms * iters / 0.020 / 1e12, 3))
+    assert math.isclose(mf["fp64_tflops"], round(24 * prisms * iters / 0.020 / 1e12, 3))
 
 
 def test_step_bytes_count_iterations_updates_and_stage_kernels():
