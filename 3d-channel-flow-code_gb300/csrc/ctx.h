@@ -51,8 +51,8 @@ struct nsmp_ctx {
     int stage32 = 0;              // 1: stage right-hand side in FP32 arithmetic
     int fp64_spmv_mf = 0;         // 1: FP64 BiCGSTAB regenerates its couplings instead of reading them
     int l2_limit_set = 0;         // 1: this context raised the persisting-L2 limit (restored by the last such context)
-    double inner_tol = 1e-1;      // FP32 residual reduction that triggers an FP64 update
-    int inner_cap = 50;           // most FP32 iterations between two FP64 updates
+    double inner_tol = 3e-2;      // FP32 residual reduction that triggers an FP64 update
+    int inner_cap = 80;           // most FP32 iterations between two FP64 updates
     int restart_every = 300;      // most FP32 iterations of one Krylov process
     int last_outer = 0;
     double* stage_buf = nullptr;  // (N_CELL,NZ) staging for transfers

@@ -567,26 +567,27 @@ __global__ void __launch_bounds__(kBlock) k_mix_scale(Mesh m, MixArgs a, RedScra
     const int rst = sc->restart, jit = sc->perturb;
     const unsigned int salt = (unsigned int)sc->outer;
     float part[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+    auto fp64_r = [&](int g) {  // the new FP64 residual, blended when theta != 1
         double r = rn[g];
         if (blend) {
             r = fma(th, r - ro[g], ro[g]);
             rn[g] = r;
             xn[g] = fma(th, xn[g] - xo[g], xo[g]);
         }
+        return r;
+    };
+    // one prism: r~ = D^-1 (r - mean r) / iscale, r^0 on a restart, partials
+    auto one = [&](int g, double r, float id, float q0in, float& rt, float& q0out) {
         const float rf = (float)((r - rm) * inv);
-        const float id = a.invD[g];
-        const float rt = rf * id;  // r~ = D^-1 r
-        a.r[g] = rt;
-        a.e[g] = 0.f;
+        rt = rf * id;  // r~ = D^-1 r
         if (rst) {  // restart: r^0 = D r0 with r0 = r, perturbed after a stalled cycle
             const float d = __frcp_rn(id);
             const float ru = rt * d;
             const float q0 = jit ? ru * (1.0f + 0.5f * shadow_jitter((unsigned int)g, salt)) : ru;
-            a.r0[g] = q0 * d;
+            q0out = q0 * d;
             part[5] = fmaf(q0, ru, part[5]);
         } else {
-            part[5] = fmaf(a.r0[g], rt, part[5]);  // (r0, r) = (r^0, r~)
+            part[5] = fmaf(q0in, rt, part[5]);  // (r0, r) = (r^0, r~)
         }
         const float ra = rf + rmi;
         part[0] += fabsf(ra);
@@ -594,6 +595,38 @@ __global__ void __launch_bounds__(kBlock) k_mix_scale(Mesh m, MixArgs a, RedScra
         part[2] += ra;
         part[3] += fabsf(rf);
         part[4] = fmaf(rf, rf, part[4]);
+    };
+    // four prisms a thread with 16- and 32-byte loads (the pass is latency-
+    // bound with one prism a thread), then the remainder one by one
+    const int n4 = m.nprism >> 2;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
+        const int g = 4 * i;
+        double r[4];
+        if (blend) {
+#pragma unroll
+            for (int l = 0; l < 4; ++l) r[l] = fp64_r(g + l);
+        } else {
+            const double2 r01 = reinterpret_cast<const double2*>(rn)[2 * i];
+            const double2 r23 = reinterpret_cast<const double2*>(rn)[2 * i + 1];
+            r[0] = r01.x; r[1] = r01.y; r[2] = r23.x; r[3] = r23.y;
+        }
+        const float4 id = reinterpret_cast<const float4*>(a.invD)[i];
+        const float4 qi = rst ? make_float4(0.f, 0.f, 0.f, 0.f) : reinterpret_cast<const float4*>(a.r0)[i];
+        float4 rt, qo;
+        one(g, r[0], id.x, qi.x, rt.x, qo.x);
+        one(g + 1, r[1], id.y, qi.y, rt.y, qo.y);
+        one(g + 2, r[2], id.z, qi.z, rt.z, qo.z);
+        one(g + 3, r[3], id.w, qi.w, rt.w, qo.w);
+        reinterpret_cast<float4*>(a.r)[i] = rt;
+        reinterpret_cast<float4*>(a.e)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (rst) reinterpret_cast<float4*>(a.r0)[i] = qo;
+    }
+    for (int g = 4 * n4 + blockIdx.x * blockDim.x + threadIdx.x; g < m.nprism; g += gridDim.x * blockDim.x) {
+        float rt, qo = 0.f;
+        one(g, fp64_r(g), a.invD[g], rst ? 0.f : a.r0[g], rt, qo);
+        a.r[g] = rt;
+        a.e[g] = 0.f;
+        if (rst) a.r0[g] = qo;
     }
     double tot[6];
     if (grid_reduce_f<6>(part, rs, tot) && threadIdx.x == 0) {
@@ -636,6 +669,11 @@ __global__ void k_mix_setup(Mesh m, const double* __restrict__ invD, float* __re
 
 }  // namespace
 
+// Offset of the shadow residual in the block that starts with D^-1: both are
+// loaded as float4 at 4-aligned compact indices, so r^0 starts on a 16-byte
+// boundary.
+static size_t r0_offset(size_t nprism) { return (nprism + 3) / 4 * 4; }
+
 int mixed_alloc(nsmp_ctx* c) {
     const HostLayout& L = c->L;
     const size_t ncf = (size_t)L.N0 * L.NZ;
@@ -653,8 +691,9 @@ int mixed_alloc(nsmp_ctx* c) {
     // D^-1 and the shadow residual are read by both passes of every
     // iteration and never written inside a Krylov process: one block, so a
     // single L2 access-policy window can keep them resident
-    CK(dalloc((void**)&c->invD32, 2 * ncf * sizeof(float)));
-    c->r032 = c->invD32 + ncf;
+    const size_t np = (size_t)L.N0 * (L.NZ - 2);
+    CK(dalloc((void**)&c->invD32, (r0_offset(np) + np) * sizeof(float)));
+    c->r032 = c->invD32 + r0_offset(np);
     CK(dalloc((void**)&c->d_ppe32, sizeof(ColPPE32) * L.N0));
     const int nzp = (L.NZ - 2 + 3) / 4 * 4;  // interior layers, rounded up to a float4
     CK(dalloc((void**)&c->lev32, sizeof(float) * (3 * nzp + 4 * (size_t)L.NZ)));
@@ -797,7 +836,7 @@ struct L2Window {
 int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     const Mesh& m = c->mesh;
     cudaStream_t st = c->stream;
-    L2Window l2win(c, (size_t)m.nprism * sizeof(float) + (size_t)m.N0 * m.NZ * sizeof(float));
+    L2Window l2win(c, (r0_offset((size_t)m.nprism) + (size_t)m.nprism) * sizeof(float));
     if (m.NZI & 1) {
         c->err = "mixed precision needs an even number of layers";
         return NSMP_ERR_UNSUPPORTED;
@@ -808,7 +847,7 @@ int run_pressure_mixed(nsmp_ctx* c, const double* pf, const double** x_final) {
     const int g_pv = quad ? grid_occ(c, k_in_pv<4>, m.nprism / L) : grid_occ(c, k_in_pv<2>, m.nprism / L);
     const int g_st = quad ? grid_occ(c, k_in_st<4>, m.nprism / L) : grid_occ(c, k_in_st<2>, m.nprism / L);
     const int g_in = grid_occ(c, k_mix_init, m.nprism), g_u = grid_occ(c, k_mix_update, m.nprism);
-    const int g_sc = grid_occ(c, k_mix_scale, m.nprism);
+    const int g_sc = grid_occ(c, k_mix_scale, (m.nprism + 3) / 4);
     MixArgs a{c->rhsp, pf, c->b64, c->r, c->x, c->xa, c->xb, c->r32, c->r032, c->p32[0], c->p32[1], c->v32[0],
               c->v32[1], c->s32, c->t32, c->e32, c->invD32, c->d_ppe32, c->lev32,
               (m.NZI + 3) / 4 * 4, reinterpret_cast<const float4*>(c->lev32 + 3 * ((m.NZI + 3) / 4 * 4)),

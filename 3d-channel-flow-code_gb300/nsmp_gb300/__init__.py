@@ -447,7 +447,7 @@ class Solver:
     def set_precision(self, mode):
         self._check(self.L.nsmp_set_precision(self.h, int(mode)))
 
-    def set_inner_solver(self, inner_tol=1e-1, inner_cap=50, restart_every=300):
+    def set_inner_solver(self, inner_tol=3e-2, inner_cap=80, restart_every=300):
         self._check(self.L.nsmp_set_inner_solver(self.h, float(inner_tol), int(inner_cap), int(restart_every)))
 
     def prof_enable(self, on=True):

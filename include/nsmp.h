@@ -196,7 +196,7 @@ int nsmp_set_precision(nsmp_ctx* ctx, int mode);
 int nsmp_mass_diag_noalloc(nsmp_ctx* ctx, double out[4]);
 /* NSMP_MIXED pressure solver.  The FP32 BiCGSTAB hands its correction e to
  * FP64 when its residual fell by inner_tol since the last hand-over (default
- * 1e-1) or after inner_cap iterations (default 50): x += e, and the FP32
+ * 3e-2) or after inner_cap iterations (default 80): x += e, and the FP32
  * residual is replaced by the FP64 residual b - A x.  A correction that
  * raised |b - A x|_2 more than 2x is cut to the step that minimises it and
  * the Krylov process restarts with a perturbed shadow residual; it also
