@@ -8,8 +8,10 @@ What is pinned, and how:
   * solver parity -- BiCGSTAB residual histories agree to <= 1e-11 for the
     first 12 iterations; at the reference tolerance 1e-10 the iteration
     counts stay within the spread the oracle shows against itself when only
-    the order of its global sums changes (up to 20 %), with fields at the
-    solver tolerance (u, v, w <= 1e-9, p <= 1e-8);
+    the order of its global sums changes (up to 20 %), and the fields within
+    the solver tolerance (u, v, w <= 1e-9, p <= 1e-8) or three times that
+    self-spread, whichever is larger (on the 32,768-prism case the oracle's
+    p moves by 1.8e-8 when its sums are reversed);
   * time integration -- Euler->AB2, RK2 and RK3 over several steps, and
     100 RK3 steps of the 32,768-prism case at relative L2 <= 1e-8;
   * the 1,048,576-prism case (one RK3 step) at both tolerances.
@@ -40,22 +42,36 @@ def _pair(prm, mesh, seed=1):
 
 
 def _errors(o, s):
+    """Relative L2 differences of every field between the oracle o and s (the
+    GPU solver, or a second oracle)."""
+    get = s.download if isinstance(s, ng.Solver) else (lambda f: s.get(_ORC[f]))
     e = {}
     for fg, fo in CELL_FIELDS:
-        a, b = s.download(fg), o.get(fo)
+        a, b = get(fg), o.get(fo)
         e[f"cell{fg}"] = rel_l2(interior(a, o.n0), interior(b, o.n0))
         # ghost columns (periodic images) and wall layers as well
         e[f"full{fg}"] = rel_l2(a, b)
     for fg, fo in FACE_FIELDS:
-        a, b = s.download(fg), o.get(fo)
+        a, b = get(fg), o.get(fo)
         e[f"face{fg}"] = rel_l2(a[:, 1:-1], b[:, 1:-1])
     return e
 
 
-def _compare(o, s, tol, what="", tol_p=None):
+_ORC = {fg: fo for fg, fo in CELL_FIELDS + FACE_FIELDS}
+
+
+def _compare(o, s, tol, what="", tol_p=None, spread=None):
+    """Every field of s within tol of the oracle (tol_p for p).  With
+    `spread` (the differences between the oracle and itself with its global
+    sums reversed, from _errors), a field may also differ by up to three
+    times that spread: at eps = 1e-10 two solves that each meet the stopping
+    test differ by the rounding of their dot products amplified by the
+    operator's conditioning, and the GPU sums in a third order."""
     e = _errors(o, s)
     lim = {k: (tol_p if (tol_p and k.endswith(str(ng.F_P)) and k.startswith(("cell", "full"))) else tol)
            for k in e}
+    if spread:
+        lim = {k: max(v, 3.0 * spread[k]) for k, v in lim.items()}
     bad = {k: v for k, v in e.items() if not v <= lim[k]}
     assert not bad, f"{what}: fields above tolerance: {bad}"
     return e
@@ -128,9 +144,9 @@ def test_one_stage_at_reference_tolerance():
     _, io = o.step(1)
     _, inf = s.step(1, 1)
     assert inf["converged"] == 1 and io["converged"] == 1
-    rev, _ = oracle_iterations(prm, mesh, 1, True)
+    rev, orev = oracle_iterations(prm, mesh, 1, True)
     assert_iterations_within_oracle_spread([inf["iters"]], [io["iters"]], rev)
-    _compare(o, s, 1e-9, "eps=1e-10", tol_p=1e-8)
+    _compare(o, s, 1e-9, "eps=1e-10", tol_p=1e-8, spread=_errors(o, orev))
 
 
 def rk3_stagewise(s):
@@ -160,9 +176,9 @@ def test_config0_rk3_at_reference_tolerance():
     o, s = _pair(prm, mesh)
     _, io = o.step(3)
     its = rk3_stagewise(s)
-    rev, _ = oracle_iterations(prm, mesh, 3, True)
+    rev, orev = oracle_iterations(prm, mesh, 3, True)
     assert_iterations_within_oracle_spread(its, io["iters_stage"], rev)
-    _compare(o, s, 1e-9, "config0 eps=1e-10", tol_p=1e-8)
+    _compare(o, s, 1e-9, "config0 eps=1e-10", tol_p=1e-8, spread=_errors(o, orev))
 
 
 @pytest.mark.slow
@@ -181,10 +197,12 @@ def test_config1_one_step(eps, tol, tol_p):
     o, s = _pair(prm, mesh)
     _, io = o.step(3)
     its = rk3_stagewise(s)
+    spread = None
     if eps == 1e-10:
-        rev, _ = oracle_iterations(prm, mesh, 3, True)
+        rev, orev = oracle_iterations(prm, mesh, 3, True)
         assert_iterations_within_oracle_spread(its, io["iters_stage"], rev)
-    _compare(o, s, tol, f"config1 eps={eps}", tol_p=tol_p)
+        spread = _errors(o, orev)
+    _compare(o, s, tol, f"config1 eps={eps}", tol_p=tol_p, spread=spread)
 
 
 def test_config0_one_step_rk3():
