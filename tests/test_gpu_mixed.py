@@ -54,6 +54,34 @@ def test_incremental_residual_matches_recomputed():
     s.close()
 
 
+def test_recurrence_form_matches_direct_products():
+    """The p/v pass forms A D^-1 p by the recurrence v' = w - omega M w
+    (w = t + beta v) between FP64 hand-overs, and directly on the pass after
+    each hand-over.  With a hand-over after every FP32 iteration
+    (inner_cap = 1) every product is formed directly; both solves converge
+    to eps = 1e-12 on the 32,768-prism mesh and give the same fields to the
+    solver tolerance."""
+    prm, mesh = small_case(32, 16, layers=32, dt=1e-3, eps=1e-12, max_iters=50000, precision=ng.MIXED)
+    rec, _ = _start(prm, mesh)
+    direct, _ = _start(prm, mesh)
+    direct.set_inner_solver(inner_tol=0.5, inner_cap=1, restart_every=300)
+    its = {}
+    for name, s in (("recurrence", rec), ("direct", direct)):
+        it0, up0 = s.solver_counters()
+        rc, inf = s.step(3, 1)
+        it1, up1 = s.solver_counters()
+        assert rc == 0 and inf["converged"] == 1 and min(inf["e1norm"], inf["e2norm"]) < 1e-12
+        its[name] = (it1 - it0, up1 - up0)
+    # the direct run hands over after every iteration, the recurrence run rarely
+    assert its["direct"][1] >= its["direct"][0] and its["recurrence"][1] < its["recurrence"][0] / 10, its
+    n0 = prm["n0"]
+    for f in (ng.F_U, ng.F_V, ng.F_W):
+        assert rel_l2(interior(rec.download(f), n0), interior(direct.download(f), n0)) <= 1e-9
+    assert rel_l2(interior(rec.download(ng.F_P), n0), interior(direct.download(ng.F_P), n0)) <= 1e-7
+    rec.close()
+    direct.close()
+
+
 def test_mixed_matches_fp64_after_steps():
     """32,768-prism mesh, 20 RK3 steps at eps = 1e-10: mixed vs FP64 GPU."""
     prm, mesh = small_case(32, 16, layers=32, dt=1e-3)
