@@ -297,6 +297,11 @@ class StateBuffers:
     def upload(self, s, flag):
         s.upload_state(*self.cells, self.faces, self.hist, flag)
 
+    def copy_from(self, other):
+        for a, b in zip(self.cells + self.faces + self.hist, other.cells + other.faces + other.hist):
+            np.copyto(a, b)
+        self.flag = other.flag
+
 
 def timed_region(s, ng, torch, stream, steps, pg, local, profile=False):
     """K RK3 steps between CUDA events on the library's stream.  With
@@ -338,6 +343,9 @@ def timed_region(s, ng, torch, stream, steps, pg, local, profile=False):
 # solver's FP64 hand-over kernels, which act once per refinement update.
 ITER_KERNELS = ("k_bicg_p", "k_bicg_spmv_v", "k_bicg_s", "k_bicg_spmv_t", "k_bicg_x", "k_in_pv", "k_in_st")
 UPDATE_KERNELS = ("k_mix_update", "k_mix_scale")
+
+# End-to-end replays of the timed steps; the median is reported.
+E2E_REPLAYS = 3
 
 
 def step_bytes(prof, iters, updates, steps, prisms, mixed):
@@ -497,22 +505,33 @@ def run_ours(args):
     # output state, which is the next step's input.  The K steps are those of
     # the timed region, so the solver work is the same and the copies are
     # what is added; the replay ends on the timed region's final u, bit for
-    # bit, when upload and download are exact.
-    st_out = StateBuffers(torch, ng, s, prm)
-    st_in, flag = snap, snap.flag
-    torch.cuda.synchronize()
-    barrier(pg)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        st_in.upload(s, flag)
-        s.step(3, 1)
-        st_out.download(s)
-        flag = st_out.flag
-        st_in, st_out = st_out, st_in
-    torch.cuda.synchronize()
-    t_e2e = max_over_ranks(pg, time.perf_counter() - t0)
+    # bit, when upload and download are exact.  The replay runs E2E_REPLAYS
+    # times and the median wall-clock time is reported: the host cores are
+    # shared, and a single replay of a few steps has read 4-25 ms a step of
+    # copy overhead for about 7 ms of copies.  The replays ping-pong between
+    # two buffers of their own, so `snap` stays the timed region's start
+    # state for the CPU baseline below.
+    st_a = StateBuffers(torch, ng, s, prm)
+    st_b = StateBuffers(torch, ng, s, prm)
+    t_reps, e2e_exact = [], True
+    for _ in range(E2E_REPLAYS):
+        st_a.copy_from(snap)
+        st_in, st_out, flag = st_a, st_b, snap.flag
+        torch.cuda.synchronize()
+        barrier(pg)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            st_in.upload(s, flag)
+            s.step(3, 1)
+            st_out.download(s)
+            flag = st_out.flag
+            st_in, st_out = st_out, st_in
+        torch.cuda.synchronize()
+        t_reps.append(max_over_ranks(pg, time.perf_counter() - t0))
+        e2e_exact = e2e_exact and bool(np.array_equal(st_in.cells[0], u_end))
+    t_e2e = float(np.median(t_reps))
     e2e_value = job_value(world, prisms, args.steps, t_e2e * 1e3)
-    e2e_exact = bool(np.array_equal(st_in.cells[0], u_end))
+    e2e_values = [round(job_value(world, prisms, args.steps, t * 1e3), 3) for t in t_reps]
     h2d = d2h = st_in.nbytes
 
     # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
@@ -544,7 +563,9 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": args.steps,
-                    "replay": "the timed steps from their start state, full state up and down each step",
+                    "replay": "the timed steps from their start state, full state up and down each step; "
+                              f"median of {E2E_REPLAYS} replays (host wall clock)",
+                    "replay_values": e2e_values,
                     "replay_matches_timed_u_bitwise": e2e_exact},
             "clocks": r["clocks"],
             "gpu_launches": r["launches"],
