@@ -171,8 +171,9 @@ __device__ __forceinline__ void stv(float* p, size_t i, const FV<L>& o) {
 //   M p~' = M (s~ - om t~ + beta (p~ - om v~)) = w - om M w,  w = t~ + beta v~,
 // so a lateral neighbour contributes two loads (t~, v~) instead of four
 // (s~, t~, p~, v~).  The recurrence carries the rounding of the earlier v~
-// forward; every FP64 update is followed by a mode-1 pass, which forms
-// M p~ directly again.
+// forward; every FP64 update is followed by a mode-1 pass (mode 0 after a
+// restart), which forms M p~ directly again, so the recurrence spans at most
+// inner_cap iterations.
 template <int MODE>
 __device__ __forceinline__ float pv_in1(const MixArgs& a, const float* pin, const float* vin, float beta, float om,
                                         size_t i) {  // operator input at one point: p~ (modes 0, 1) or w (mode 2)
